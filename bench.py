@@ -1,0 +1,467 @@
+#!/usr/bin/env python
+"""Benchmark of the likelihood + branch-length-gradient path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload batched-hky-g4|gtr-g4|restriction|restriction-g4-bd|protein-g4]
+
+One step = one logL + gradient evaluation of the whole workload (every instance,
+every site, every rate category) after a new set of branch lengths, i.e. one
+leapfrog step of a sampler.  Metric: site-node updates/s, units = sum over
+instances of (N_i - 1) * S_i * C.
+
+Default workload: 256 independent HKY+G4 instances of uneven size in one launch
+(T ~ logU[16, 1024] taxa, S ~ logU[500, 50000] sites, kappa ~ LogNormal(1, 0.5)),
+FP32-scaled path, compared with the plain FP64 GPU path on the same inputs.
+
+value: device-resident inputs (branch lengths already in HBM), CUDA events on the
+engine's stream around each step, L2 flushed (512 MB write) between steps outside
+the events.  e2e: the same step through the C ABI with host buffers (branch
+lengths in, ll and gradient out, copies inside the timed region).
+--impl reference: the CPU restatement of the reference's loops (FP64, OpenMP, all
+host cores) on a bounded sample of the same workload each step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "mcphylo.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "logL+grad site-node updates/s, FP32-scaled vs plain FP64 GPU at ≤1e-6 rel err"
+UNIT = "site-node updates/s"
+
+
+# ----------------------------------------------------------------------------- workloads
+def make_workload(name, workers):
+    from mcphylo_gb300 import simulate
+    if name == "batched-hky-g4":
+        insts = simulate.hky_batch(seed=4, n=256, workers=workers)
+        cfg = {"workload": "batched-hky-g4", "instances": 256, "taxa": "logU[16,1024]",
+               "sites": "logU[500,50000]", "model": "HKY+G4 (shape 0.5), kappa~LogNormal(1,0.5)",
+               "states": 4, "rates": 4}
+    elif name == "gtr-g4":
+        insts = [simulate.gtr_gamma(S=100_000, with_weights=False)]
+        cfg = {"workload": "gtr-g4", "taxa": 128, "sites": 100_000, "model": "GTR+G4 (shape 0.5)",
+               "states": 4, "rates": 4}
+    elif name == "restriction":
+        insts = [simulate.restriction_small()]
+        cfg = {"workload": "restriction", "taxa": 32, "sites": 1000, "model": "Restriction",
+               "states": 2, "rates": 1}
+    elif name == "restriction-g4-bd":
+        insts = [simulate.restriction_gamma_bd()]
+        cfg = {"workload": "restriction-g4-bd", "taxa": 512, "sites": 20_000,
+               "model": "Restriction+G4 (shape 1)", "states": 2, "rates": 4}
+    elif name == "protein-g4":
+        insts = [simulate.protein_gamma()]
+        cfg = {"workload": "protein-g4", "taxa": 256, "sites": 50_000,
+               "model": "GTR20+G4 (shape 0.5)", "states": 20, "rates": 4}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    cfg["units_per_step"] = int(sum(i.units() for i in insts))
+    return insts, cfg
+
+
+def make_engine(insts, precision, tiles=None):
+    import mcphylo_gb300 as mp
+    e = mp.Engine(insts[0].K, len(insts[0].rates), precision, n_instances=len(insts))
+    if tiles:
+        e.set_tiles(*tiles)
+    for i, b in enumerate(insts):
+        e.set_tree(b.parent, b.blen, i)
+        e.set_codes(b.codes, b.leaf_nums, i)
+        e.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, i)
+    return e
+
+
+def algorithmic_bytes(insts, spt, real_bytes):
+    """Bytes the fused kernel must move per evaluation: every post-order partial of
+    an internal non-root step written once and read once, the leaf state codes read
+    once, the per-item gradient partials written once."""
+    import mcphylo_gb300 as mp
+    total = 0
+    K = insts[0].K
+    Kp = 2 if K <= 2 else 4 if K <= 4 else 8 if K <= 8 else 20 if K <= 20 else 32
+    code_b = 1 if Kp <= 8 else 4
+    for b in insts:
+        info = mp.schedule_info(b.parent)
+        C = len(b.rates)
+        lanes = b.S * C
+        blocks = -(-b.S // (32 * spt))
+        total += 2 * lanes * (info["internal"] - 1) * Kp * real_bytes
+        total += len(b.leaf_nums) * b.S * code_b
+        total += C * blocks * (b.N - 1) * real_bytes
+    return total
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for ln in open(self.path):
+                f = [x.strip() for x in ln.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- CPU sample
+def cpu_sample(insts, seconds, max_sites=2000):
+    """The oracle (FP64 restatement of the reference loops, OpenMP over all host
+    cores) on the workload's instances in order, each truncated to its first
+    max_sites sites, until ``seconds`` have elapsed."""
+    from oracle import pyoracle as O
+    from mcphylo_gb300 import simulate
+    O.lib()
+    units = 0
+    done = 0
+    t0 = time.perf_counter()
+    for b in insts:
+        S = min(b.S, max_sites)
+        sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums, b.codes[:, :S], b.U, b.D,
+                                b.Uinv, b.mu, b.pi, b.rates)
+        x = sub.tensor()
+        t = O.tree_from_parent(sub.parent, sub.blen)
+        ts = time.perf_counter()
+        O.gradlogpdf(t, x, sub.pi, (sub.U, sub.D, sub.Uinv, sub.mu), sub.rates)
+        units += sub.units()
+        done += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+        _ = ts
+    el = time.perf_counter() - t0
+    return units / el, {"instances": done, "max_sites": max_sites, "units": units,
+                        "seconds": round(el, 3), "threads": O.num_threads()}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    insts, cfg = make_workload(args.workload, workers=min(16, os.cpu_count() or 1))
+    from oracle import pyoracle as O
+    from mcphylo_gb300 import simulate
+    O.lib()
+    # one step = the oracle's logL + gradient on a fixed bounded sample
+    sample = []
+    budget = args.ref_units
+    for b in insts:
+        S = min(b.S, 2000)
+        sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums, b.codes[:, :S], b.U, b.D,
+                                b.Uinv, b.mu, b.pi, b.rates)
+        sample.append((O.tree_from_parent(sub.parent, sub.blen), sub.tensor(), sub))
+        budget -= sub.units()
+        if budget <= 0:
+            break
+    units = sum(s[2].units() for s in sample)
+
+    def step():
+        for t, x, s in sample:
+            O.gradlogpdf(t, x, s.pi, (s.U, s.D, s.Uinv, s.mu), s.rates)
+
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    v = units / (ms / 1e3)
+    desc = (f"{len(sample)} of the workload's instances, first <=2000 sites each, "
+            f"{units} units per step")
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded simulation)", "config": cfg,
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+                            "sample": desc},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "the reference is Julia and cannot run here; this is the C/OpenMP FP64 "
+                   "restatement of its loops (oracle/oracle.c)"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def autotune(insts, steps=2):
+    """Sites per thread x threads per block of the fused kernel, best device time."""
+    K = insts[0].K
+    cands = [(1, 256), (2, 256), (2, 128), (4, 128), (1, 128), (4, 256)] if K <= 4 else \
+        [(1, 256), (2, 128), (1, 128)] if K <= 8 else [(1, 128), (1, 64)]
+    res = {}
+    for spt, tpb in cands:
+        e = make_engine(insts, "f32", (spt, tpb))
+        e.enable_timing(True)
+        e.logpdf_grad()
+        ts = []
+        for _ in range(steps):
+            e.logpdf_grad()
+            ts.append(e.timing()["prune_ms"])
+        res[f"{spt}x{tpb}"] = min(ts)
+        e.close()
+    best = min(res, key=res.get)
+    spt, tpb = (int(x) for x in best.split("x"))
+    return (spt, tpb), res
+
+
+def run_gpu(args, rank, world):
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    insts, cfg = make_workload(args.workload, workers=min(16, os.cpu_count() or 1))
+    units = cfg["units_per_step"]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    tiles, tune = autotune(insts) if args.tiles == "auto" else \
+        (tuple(int(x) for x in args.tiles.split("x")), {})
+    e = make_engine(insts, "f32", tiles)
+    M = len(insts)
+    off = e.grad_offsets()
+    G = int(off[-1])
+    stream = torch.cuda.current_stream()
+    e.set_stream(stream.cuda_stream)
+    e.enable_timing(True)
+
+    # branch-length sets for every step (leapfrog-like multiplicative moves)
+    rng = np.random.default_rng(123 + rank)
+    base = np.concatenate([b.blen for b in insts])
+    nsets = args.warmup + args.steps
+    host_sets = [base * np.exp(0.05 * rng.standard_normal(base.shape)) for _ in range(nsets)]
+    dev_sets = torch.tensor(np.stack(host_sets), dtype=torch.float64, device="cuda")
+    d_ll = torch.zeros(M, dtype=torch.float64, device="cuda")
+    d_grad = torch.zeros(G, dtype=torch.float64, device="cuda")
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 512 MB > L2
+
+    def dev_step(k):
+        e.set_all_branch_lengths_device(dev_sets[k].data_ptr())
+        e.logpdf_grad_device(d_ll.data_ptr(), d_grad.data_ptr())
+
+    for k in range(args.warmup):
+        flush.zero_()
+        dev_step(k)
+    e.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    prune_ms, build_ms, red_ms = [], [], []
+    ll32 = []
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            dev_step(args.warmup + i)
+            ends[i].record(stream)
+            e.synchronize()
+            t = e.timing()
+            prune_ms.append(t["prune_ms"])
+            build_ms.append(t["build_p_ms"])
+            red_ms.append(t["reduce_ms"])
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    clocks = clk.summary()
+    step_ms = [s.elapsed_time(t) for s, t in zip(starts, ends)]
+    ms = statistics.mean(step_ms)
+    if dist is not None:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = units * world / (ms / 1e3)
+    ll32_last = d_ll.cpu().numpy().copy()
+    g32_last = d_grad.cpu().numpy().copy()
+
+    # e2e through the C ABI with host buffers
+    ll_h = np.zeros(M)
+    g_h = np.zeros(G)
+    e.set_stream(0)
+    e.enable_timing(False)
+    for k in range(min(2, args.warmup)):
+        e.set_all_branch_lengths(host_sets[k])
+        e.logpdf_grad(ll_h, g_h)
+    e2e_t = []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.set_all_branch_lengths(host_sets[args.warmup + i])
+        e.logpdf_grad(ll_h, g_h)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * statistics.mean(e2e_t)
+    e2e = {"value": units * world / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+           "h2d_bytes_per_step": int(base.nbytes), "d2h_bytes_per_step": int((M + G) * 8),
+           "path": "mcphy_batch_set_all_branch_lengths + mcphy_batch_logpdf_grad (host arrays)"}
+    e.close()
+    del e
+
+    # plain FP64 GPU path on the same inputs (last step's branch lengths)
+    fp64 = None
+    err = None
+    if not args.no_fp64:
+        e64 = make_engine(insts, "f64")
+        e64.enable_timing(True)
+        last = host_sets[args.warmup + args.steps - 1]
+        e64.set_all_branch_lengths(last)
+        ll64, g64 = e64.logpdf_grad()
+        t64 = []
+        for _ in range(args.fp64_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e64.logpdf_grad()
+            tm = e64.timing()
+            t64.append(tm["build_p_ms"] + tm["prune_ms"] + tm["reduce_ms"])
+        ms64 = statistics.mean(t64)
+        fp64 = {"value": units * world / (ms64 / 1e3), "ms_per_step": ms64,
+                "speedup_fp32_over_fp64": (units / (ms / 1e3)) / (units / (ms64 / 1e3))}
+        ll64 = np.atleast_1d(ll64)
+        rel_tot = abs(ll32_last.sum() - ll64.sum()) / abs(ll64.sum())
+        rel_inst = np.max(np.abs(ll32_last - ll64) / np.abs(ll64))
+        gscale = np.zeros_like(g64)
+        for i in range(M):
+            s = slice(off[i], off[i + 1])
+            gscale[s] = np.maximum(np.abs(g64[s]), 1e-2 * np.abs(g64[s]).max())
+        rel_g = float(np.max(np.abs(g32_last - g64) / gscale))
+        err = {"logl_total_rel": float(rel_tot), "logl_max_instance_rel": float(rel_inst),
+               "grad_max_entry_rel": rel_g, "grad_floor": "1e-2 x max |g| of the instance",
+               "within_1e-6": bool(rel_inst <= 1e-6)}
+        e64.close()
+
+    real_b = 4
+    alg = algorithmic_bytes(insts, tiles[0], real_b)
+    pr = statistics.mean(prune_ms)
+    achieved = alg / (pr / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "prune_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            if tj.get("workload") == cfg["workload"]:
+                traffic = tj.get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "kernel": "prune_kernel<4,float,%d>" % tiles[0],
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": alg,
+                "algorithmic_bytes_per_unit": alg / units,
+                "kernel_ms": pr, "share_of_step": pr / ms}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, info = cpu_sample(insts, args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
+               "sample": f"oracle on {info['instances']} instances, first <={info['max_sites']} "
+                         f"sites each, {info['units']} units in {info['seconds']} s"}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded simulation down Yule trees)",
+           "config": dict(cfg, tiles={"sites_per_thread": tiles[0], "threads_per_block": tiles[1]},
+                          l2="flushed between steps (512 MB write, outside the timed events)",
+                          parallelism="replicas" if world > 1 else "single GPU"),
+           "clocks": clocks, "e2e": e2e, "gpu_launches": 4 * args.steps,
+           "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64, "fp32_error": err,
+           "kernel_ms": {"build_transition": statistics.mean(build_ms), "prune": pr,
+                         "reduce": statistics.mean(red_ms)},
+           "autotune_prune_ms": tune, "wall_s_timed_loop": wall}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched-hky-g4")
+    ap.add_argument("--tiles", default="auto", help="auto or SPTxTPB, e.g. 2x256")
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-units", type=float, default=6e7,
+                    help="units per step of the reference arm's bounded sample")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gpu(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,903 @@
+// C-ABI of libmcphylo_gpu.so: engine handles, validation, device layout and the
+// launch sequence of one evaluation.  Declarations and the reference functions
+// each entry point replaces are in include/mcphylo_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "mcphy_internal.h"
+#include "mcphylo_gpu.h"
+
+using namespace mcphy;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct Inst {
+    // tree
+    int64_t N = 0;
+    std::vector<int64_t> parent;
+    std::vector<double> blen;
+    bool has_tree = false;
+    // data
+    int64_t S = 0;
+    int64_t data_N = 0;
+    std::vector<int64_t> leaf_nums;
+    bool dense = false;
+    std::vector<uint32_t> codes;   // [leaf_row][S]
+    std::vector<double> dvals;     // [leaf_row][S][K]
+    bool has_data = false;
+    // model
+    std::vector<double> U, D, Uinv, pi, rates;
+    double mu = 0.0;
+    bool has_model = false;
+};
+
+int kp_of(int K) {
+    if (K <= 2) return 2;
+    if (K <= 4) return 4;
+    if (K <= 8) return 8;
+    if (K <= 20) return 20;
+    if (K <= 32) return 32;
+    return 0;
+}
+
+bool all_finite(const double* p, int64_t n) {
+    for (int64_t i = 0; i < n; ++i)
+        if (!std::isfinite(p[i])) return false;
+    return true;
+}
+
+}  // namespace
+
+struct mcphy_engine {
+    int K = 0, Kp = 0, C = 0, prec = 0;
+    int64_t M = 0;
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<Inst> inst;
+    unsigned dirty = DIRTY_LAYOUT | DIRTY_DATA | DIRTY_BLEN | DIRTY_MODEL;
+
+    // launch shape
+    int spt_req = 0, tpb_req = 0;
+    int spt = 1, tpb = 256, blocks = 0;
+
+    // layout
+    std::vector<InstanceDesc> desc;
+    std::vector<int64_t> grad_offsets;   // M + 1
+    int64_t total_branch = 0;
+    int64_t n_items = 0;
+    int64_t n_prows = 0;
+    int32_t max_J = 0;
+    int32_t max_branch = 0;
+    int64_t units = 0;
+    int64_t warp_stride = 0;
+    int64_t pre_warp_stride = 0;
+    int32_t max_pre = 0;
+    int64_t leaf_elems = 0;
+    bool any_dense = false;
+    std::vector<SchedNode> sched_all;
+
+    DevBuf d_desc, d_sched, d_items, d_queue, d_rows, d_P, d_dP, d_codes, d_dense, d_params,
+        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter;
+    int n_split = 1;
+
+    double* h_blen = nullptr;
+    size_t h_blen_cap = 0;
+    double* h_out = nullptr;
+    size_t h_out_cap = 0;
+
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float ms[3] = {0.f, 0.f, 0.f};
+    int64_t counts[3] = {0, 0, 0};
+    std::string err;
+};
+
+namespace {
+
+int fail(mcphy_engine* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? MCPHY_ERR_OOM : MCPHY_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+int ensure(mcphy_engine* h, DevBuf& b, size_t bytes) {
+    if (bytes == 0) bytes = 256;
+    if (b.cap >= bytes) return MCPHY_OK;
+    if (b.p) {
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    size_t want = (bytes + 255) & ~size_t(255);
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        return fail(h, MCPHY_ERR_OOM,
+                    "cudaMalloc(" + std::to_string(want) + " bytes): " + cudaGetErrorString(e));
+    }
+    b.cap = want;
+    return MCPHY_OK;
+}
+
+int ensure_pinned(mcphy_engine* h, double*& p, size_t& cap, size_t n) {
+    if (n == 0) n = 1;
+    if (cap >= n) return MCPHY_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&p), n * sizeof(double));
+    if (e != cudaSuccess) {
+        p = nullptr;
+        return fail(h, MCPHY_ERR_OOM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    cap = n;
+    return MCPHY_OK;
+}
+
+int check_instance(mcphy_engine* h, int64_t i) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (i < 0 || i >= h->M) return fail(h, MCPHY_ERR_ARG, "instance index out of range");
+    return MCPHY_OK;
+}
+
+size_t real_size(const mcphy_engine* h) { return h->prec == MCPHY_PREC_F64 ? 8 : 4; }
+
+// Chooses the fused kernel's launch shape.
+void choose_tiles(mcphy_engine* h) {
+    int spt = h->spt_req;
+    if (spt == 0) spt = 1;
+    if (h->prec == MCPHY_PREC_F64) spt = (h->Kp <= 4) ? std::min(spt, 2) : 1;
+    else if (h->Kp == 8) spt = std::min(spt, 2);
+    else if (h->Kp > 8) spt = 1;
+    if (spt != 1 && spt != 2 && spt != 4) spt = 1;
+    h->spt = spt;
+    h->tpb = h->tpb_req ? h->tpb_req : 256;
+}
+
+// Rebuilds schedules, offsets, work items and device tables.
+int layout(mcphy_engine* h) {
+    choose_tiles(h);
+    const int SB = 32 * h->spt;
+    const int K = h->K, Kp = h->Kp, C = h->C;
+    h->desc.assign(h->M, InstanceDesc{});
+    h->grad_offsets.assign(h->M + 1, 0);
+    h->sched_all.clear();
+    h->max_J = 0;
+    h->max_pre = 0;
+    h->max_branch = 0;
+    h->units = 0;
+    h->any_dense = false;
+
+    int64_t sched_off = 0, p_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
+            pgrad_off = 0, blen_off = 0, nrows = 0;
+    const int64_t psize = param_size(K, Kp, C);
+    for (int64_t i = 0; i < h->M; ++i) {
+        Inst& in = h->inst[i];
+        if (in.data_N != in.N)
+            return fail(h, MCPHY_ERR_SHAPE,
+                        "instance " + std::to_string(i) + ": data has " + std::to_string(in.data_N) +
+                            " nodes, tree has " + std::to_string(in.N));
+        std::vector<int32_t> row_of(in.N, -1);
+        for (size_t l = 0; l < in.leaf_nums.size(); ++l) row_of[in.leaf_nums[l] - 1] = int32_t(l);
+        Schedule sc;
+        std::string e = build_schedule(in.N, in.parent.data(), row_of, sc);
+        if (!e.empty()) return fail(h, MCPHY_ERR_TREE, "instance " + std::to_string(i) + ": " + e);
+        if (sc.leaves.size() != in.leaf_nums.size())
+            return fail(h, MCPHY_ERR_SHAPE,
+                        "instance " + std::to_string(i) + ": tree has " +
+                            std::to_string(sc.leaves.size()) + " leaves, data has " +
+                            std::to_string(in.leaf_nums.size()));
+        InstanceDesc& d = h->desc[i];
+        d.J = sc.J;
+        d.S = int32_t(in.S);
+        d.n_blocks = int32_t((in.S + SB - 1) / SB);
+        d.S_pad = d.n_blocks * SB;
+        d.n_leaf = int32_t(in.leaf_nums.size());
+        d.n_branch = int32_t(in.N - 1);
+        d.dense = in.dense ? 1 : 0;
+        d.pre_slots = sc.pre_slots;
+        d.sched_off = sched_off;
+        d.p_off = p_off;
+        d.leaf_off = leaf_off;
+        d.param_off = param_off;
+        d.item_off = item_off;
+        d.pgrad_off = pgrad_off;
+        d.blen_off = blen_off;
+        d.grad_off = blen_off;
+        h->sched_all.insert(h->sched_all.end(), sc.nodes.begin(), sc.nodes.end());
+        sched_off += sc.J;
+        p_off += int64_t(d.n_branch + 1) * C * Kp * Kp;
+        leaf_off += int64_t(d.n_leaf) * d.S_pad * (in.dense ? Kp : 1);
+        param_off += psize;
+        const int64_t items = int64_t(C) * d.n_blocks;
+        item_off += items;
+        pgrad_off += items * d.n_branch;
+        blen_off += d.n_branch;
+        nrows += d.n_branch + 1;
+        h->grad_offsets[i + 1] = blen_off;
+        h->max_J = std::max(h->max_J, sc.J);
+        h->max_pre = std::max(h->max_pre, sc.pre_slots);
+        h->max_branch = std::max(h->max_branch, d.n_branch);
+        h->units += int64_t(d.n_branch) * in.S * C;
+        h->any_dense = h->any_dense || in.dense;
+    }
+    h->total_branch = blen_off;
+    h->n_items = item_off;
+    h->n_prows = nrows;
+    h->leaf_elems = leaf_off;
+    if (h->n_items >= (int64_t(1) << 31)) return fail(h, MCPHY_ERR_ARG, "too many work items");
+
+    // work items and the order warps take them: largest trees first
+    std::vector<int2> items(h->n_items);
+    std::vector<int2> rows(nrows);
+    int64_t rr = 0;
+    for (int64_t i = 0; i < h->M; ++i) {
+        const InstanceDesc& d = h->desc[i];
+        for (int64_t q = 0; q < int64_t(C) * d.n_blocks; ++q)
+            items[d.item_off + q] = make_int2(int(i), int(q));
+        for (int b = 0; b <= d.n_branch; ++b) rows[rr++] = make_int2(int(i), b);
+    }
+    std::vector<int64_t> order(h->M);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int64_t a, int64_t b) { return h->desc[a].J > h->desc[b].J; });
+    std::vector<int32_t> queue;
+    queue.reserve(h->n_items);
+    for (int64_t i : order) {
+        const InstanceDesc& d = h->desc[i];
+        for (int64_t q = 0; q < int64_t(C) * d.n_blocks; ++q) queue.push_back(int32_t(d.item_off + q));
+    }
+
+    const size_t rs = real_size(h);
+    int rc;
+    if ((rc = ensure(h, h->d_desc, sizeof(InstanceDesc) * h->M))) return rc;
+    if ((rc = ensure(h, h->d_sched, sizeof(SchedNode) * h->sched_all.size()))) return rc;
+    if ((rc = ensure(h, h->d_items, sizeof(int2) * items.size()))) return rc;
+    if ((rc = ensure(h, h->d_queue, sizeof(int32_t) * queue.size()))) return rc;
+    if ((rc = ensure(h, h->d_rows, sizeof(int2) * rows.size()))) return rc;
+    if ((rc = ensure(h, h->d_P, rs * size_t(p_off)))) return rc;
+    if ((rc = ensure(h, h->d_dP, rs * size_t(p_off)))) return rc;
+    if ((rc = ensure(h, h->d_params, sizeof(double) * size_t(param_off)))) return rc;
+    if ((rc = ensure(h, h->d_blen, sizeof(double) * size_t(h->total_branch)))) return rc;
+    if ((rc = ensure(h, h->d_pgrad, rs * size_t(pgrad_off)))) return rc;
+    int64_t max_items = 0;
+    for (const InstanceDesc& d : h->desc) max_items = std::max<int64_t>(max_items, int64_t(C) * d.n_blocks);
+    h->n_split = int(std::min<int64_t>(64, std::max<int64_t>(1, (max_items + 127) / 128)));
+    if ((rc = ensure(h, h->d_part, sizeof(double) * size_t(h->n_split) *
+                                       size_t(h->M + h->total_branch))))
+        return rc;
+    if ((rc = ensure(h, h->d_pll, sizeof(double) * size_t(h->n_items)))) return rc;
+    if ((rc = ensure(h, h->d_out, sizeof(double) * size_t(h->M + h->total_branch)))) return rc;
+    if ((rc = ensure(h, h->d_counter, 256))) return rc;
+    const size_t code_bytes = (Kp <= 8) ? 1 : 4;
+    if ((rc = ensure(h, h->d_codes, code_bytes * size_t(h->leaf_elems)))) return rc;
+    if ((rc = ensure(h, h->d_dense, h->any_dense ? rs * size_t(h->leaf_elems) : 256))) return rc;
+    if ((rc = ensure_pinned(h, h->h_blen, h->h_blen_cap, size_t(h->total_branch)))) return rc;
+    if ((rc = ensure_pinned(h, h->h_out, h->h_out_cap, size_t(h->M + h->total_branch)))) return rc;
+
+    CK(cudaMemcpy(h->d_desc.p, h->desc.data(), sizeof(InstanceDesc) * h->M, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_sched.p, h->sched_all.data(), sizeof(SchedNode) * h->sched_all.size(),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_items.p, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_queue.p, queue.data(), sizeof(int32_t) * queue.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_rows.p, rows.data(), sizeof(int2) * rows.size(), cudaMemcpyHostToDevice));
+
+    // persistent grid: as many resident warps as the SMs hold, never more than items
+    int bps = 0;
+    cudaError_t oe = (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
+                                                  : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
+    if (oe != cudaSuccess || bps < 1) bps = 1;
+    const int wpb = h->tpb / 32;
+    int64_t blocks = int64_t(bps) * h->sm_count;
+    blocks = std::min<int64_t>(blocks, (h->n_items + wpb - 1) / wpb);
+    blocks = std::max<int64_t>(blocks, 1);
+    h->warp_stride = int64_t(h->max_J) * h->spt * 32 * Kp;
+    h->pre_warp_stride = int64_t(h->max_pre) * h->spt * 32 * Kp;
+    // keep the scratch within half of the free device memory
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t per_block = size_t(wpb) * size_t(h->warp_stride + h->pre_warp_stride) * rs;
+    const size_t have = free_b + h->d_post.cap + h->d_pre.cap;
+    while (blocks > 1 && per_block * size_t(blocks) > have / 2) blocks /= 2;
+    h->blocks = int(blocks);
+    const size_t post_b = size_t(blocks) * wpb * h->warp_stride * rs;
+    const size_t pre_b = size_t(blocks) * wpb * h->pre_warp_stride * rs;
+    if ((rc = ensure(h, h->d_post, post_b))) return rc;
+    if ((rc = ensure(h, h->d_pre, pre_b))) return rc;
+    h->counts[2] = int64_t(post_b + pre_b);
+    h->dirty |= DIRTY_DATA | DIRTY_BLEN | DIRTY_MODEL;
+    h->dirty &= ~unsigned(DIRTY_LAYOUT);
+    return MCPHY_OK;
+}
+
+int upload_data(mcphy_engine* h) {
+    const int K = h->K, Kp = h->Kp;
+    const uint32_t allmask = (K == 32) ? 0xffffffffu : ((1u << K) - 1u);
+    const bool f64 = h->prec == MCPHY_PREC_F64;
+    std::vector<uint8_t> c8;
+    std::vector<uint32_t> c32;
+    std::vector<float> df;
+    std::vector<double> dd;
+    if (Kp <= 8) c8.assign(h->leaf_elems, 0); else c32.assign(h->leaf_elems, 0);
+    if (h->any_dense) {
+        if (f64) dd.assign(h->leaf_elems, 0.0); else df.assign(h->leaf_elems, 0.f);
+    }
+    for (int64_t i = 0; i < h->M; ++i) {
+        const Inst& in = h->inst[i];
+        const InstanceDesc& d = h->desc[i];
+        for (int64_t l = 0; l < d.n_leaf; ++l) {
+            for (int64_t s = 0; s < d.S_pad; ++s) {
+                if (!in.dense) {
+                    uint32_t c = (s < in.S) ? in.codes[l * in.S + s] : allmask;
+                    const int64_t o = d.leaf_off + l * d.S_pad + s;
+                    if (Kp <= 8) c8[o] = uint8_t(c); else c32[o] = c;
+                } else {
+                    const int64_t o = d.leaf_off + (l * d.S_pad + s) * Kp;
+                    for (int k = 0; k < K; ++k) {
+                        double v = (s < in.S) ? in.dvals[(l * in.S + s) * K + k] : 1.0;
+                        if (f64) dd[o + k] = v; else df[o + k] = float(v);
+                    }
+                }
+            }
+        }
+    }
+    if (Kp <= 8) CK(cudaMemcpy(h->d_codes.p, c8.data(), c8.size(), cudaMemcpyHostToDevice));
+    else CK(cudaMemcpy(h->d_codes.p, c32.data(), c32.size() * 4, cudaMemcpyHostToDevice));
+    if (h->any_dense) {
+        if (f64) CK(cudaMemcpy(h->d_dense.p, dd.data(), dd.size() * 8, cudaMemcpyHostToDevice));
+        else CK(cudaMemcpy(h->d_dense.p, df.data(), df.size() * 4, cudaMemcpyHostToDevice));
+    }
+    h->dirty &= ~unsigned(DIRTY_DATA);
+    return MCPHY_OK;
+}
+
+int upload_model(mcphy_engine* h) {
+    const int K = h->K, Kp = h->Kp, C = h->C;
+    const int64_t psize = param_size(K, Kp, C);
+    std::vector<double> prm(size_t(psize * h->M), 0.0);
+    for (int64_t i = 0; i < h->M; ++i) {
+        const Inst& in = h->inst[i];
+        double* p = prm.data() + h->desc[i].param_off;
+        std::copy(in.U.begin(), in.U.end(), p);
+        std::copy(in.D.begin(), in.D.end(), p + K * K);
+        std::copy(in.Uinv.begin(), in.Uinv.end(), p + K * K + K);
+        p[2 * K * K + K] = in.mu;
+        std::copy(in.rates.begin(), in.rates.end(), p + 2 * K * K + K + 1);
+        std::copy(in.pi.begin(), in.pi.end(), p + 2 * K * K + K + 1 + C);
+    }
+    CK(cudaMemcpy(h->d_params.p, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice));
+    h->dirty &= ~unsigned(DIRTY_MODEL);
+    return MCPHY_OK;
+}
+
+int upload_blen(mcphy_engine* h) {
+    for (int64_t i = 0; i < h->M; ++i) {
+        const Inst& in = h->inst[i];
+        std::copy(in.blen.begin(), in.blen.end(), h->h_blen + h->desc[i].blen_off);
+    }
+    CK(cudaMemcpyAsync(h->d_blen.p, h->h_blen, sizeof(double) * size_t(h->total_branch),
+                       cudaMemcpyHostToDevice, h->stream));
+    h->dirty &= ~unsigned(DIRTY_BLEN);
+    return MCPHY_OK;
+}
+
+int prepare(mcphy_engine* h) {
+    for (int64_t i = 0; i < h->M; ++i) {
+        const Inst& in = h->inst[i];
+        if (!in.has_tree || !in.has_data || !in.has_model)
+            return fail(h, MCPHY_ERR_STATE,
+                        "instance " + std::to_string(i) + ": tree, data and model must all be set");
+    }
+    CK(cudaSetDevice(h->device));
+    int rc;
+    if (h->dirty & DIRTY_LAYOUT)
+        if ((rc = layout(h))) return rc;
+    if (h->dirty & DIRTY_DATA)
+        if ((rc = upload_data(h))) return rc;
+    if (h->dirty & DIRTY_MODEL)
+        if ((rc = upload_model(h))) return rc;
+    if (h->dirty & DIRTY_BLEN)
+        if ((rc = upload_blen(h))) return rc;
+    return MCPHY_OK;
+}
+
+// Enqueues P build, fused sweep and reduction on the handle's stream; results land
+// in d_out = [ll (M) | grad (total_branch)].
+int run(mcphy_engine* h, bool want_grad) {
+    const bool f64 = h->prec == MCPHY_PREC_F64;
+    cudaStream_t st = h->stream;
+    if (h->timing) CK(cudaEventRecord(h->ev[0], st));
+
+    BuildPArgs b{};
+    b.inst = static_cast<const InstanceDesc*>(h->d_desc.p);
+    b.rows = static_cast<const int2*>(h->d_rows.p);
+    b.n_rows = int32_t(h->n_prows);
+    b.params = static_cast<const double*>(h->d_params.p);
+    b.blen = static_cast<const double*>(h->d_blen.p);
+    b.P = h->d_P.p;
+    b.dP = h->d_dP.p;
+    b.K = h->K;
+    b.Kp = h->Kp;
+    b.C = h->C;
+    b.want_grad = want_grad ? 1 : 0;
+    CK(launch_build_p(f64, b, st));
+    if (h->timing) CK(cudaEventRecord(h->ev[1], st));
+
+    CK(cudaMemsetAsync(h->d_counter.p, 0, sizeof(int32_t), st));
+    PruneArgs a{};
+    a.inst = b.inst;
+    a.sched = static_cast<const SchedNode*>(h->d_sched.p);
+    a.items = static_cast<const int2*>(h->d_items.p);
+    a.queue = static_cast<const int32_t*>(h->d_queue.p);
+    a.n_items = int32_t(h->n_items);
+    a.counter = static_cast<int32_t*>(h->d_counter.p);
+    a.P = h->d_P.p;
+    a.dP = h->d_dP.p;
+    a.codes = h->d_codes.p;
+    a.dense = h->d_dense.p;
+    a.params = b.params;
+    a.post = h->d_post.p;
+    a.pre = h->d_pre.p;
+    a.warp_stride = h->warp_stride;
+    a.pre_warp_stride = h->pre_warp_stride;
+    a.pgrad = h->d_pgrad.p;
+    a.pll = static_cast<double*>(h->d_pll.p);
+    a.K = h->K;
+    a.C = h->C;
+    a.want_grad = want_grad ? 1 : 0;
+    CK(f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
+           : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
+    if (h->timing) CK(cudaEventRecord(h->ev[2], st));
+
+    ReduceArgs r{};
+    r.inst = b.inst;
+    r.n_inst = int32_t(h->M);
+    r.C = h->C;
+    r.n_split = h->n_split;
+    r.want_grad = want_grad ? 1 : 0;
+    r.total_branch = h->total_branch;
+    r.pgrad = a.pgrad;
+    r.pll = a.pll;
+    r.part = static_cast<double*>(h->d_part.p);
+    r.out = static_cast<double*>(h->d_out.p);
+    CK(launch_reduce(f64, r, h->max_branch, st));
+    if (h->timing) CK(cudaEventRecord(h->ev[3], st));
+    h->counts[0] = 4;   // build_transition, prune, reduce_pass1, reduce_pass2
+    h->counts[1] = h->units;
+    return MCPHY_OK;
+}
+
+int finish_timing(mcphy_engine* h) {
+    if (!h->timing) return MCPHY_OK;
+    CK(cudaEventSynchronize(h->ev[3]));
+    for (int k = 0; k < 3; ++k) CK(cudaEventElapsedTime(&h->ms[k], h->ev[k], h->ev[k + 1]));
+    return MCPHY_OK;
+}
+
+int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (!ll) return fail(h, MCPHY_ERR_ARG, "ll is NULL");
+    if (want_grad && !grad) return fail(h, MCPHY_ERR_ARG, "grad is NULL");
+    int rc;
+    if ((rc = prepare(h))) return rc;
+    if ((rc = run(h, want_grad))) return rc;
+    const size_t n = size_t(h->M) + (want_grad ? size_t(h->total_branch) : 0);
+    CK(cudaMemcpyAsync(h->h_out, h->d_out.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if ((rc = finish_timing(h))) return rc;
+    std::memcpy(ll, h->h_out, sizeof(double) * h->M);
+    if (want_grad) std::memcpy(grad, h->h_out + h->M, sizeof(double) * h->total_branch);
+    return MCPHY_OK;
+}
+
+int set_data_common(mcphy_engine* h, int64_t i, int64_t nsites, int64_t nnodes,
+                    const int64_t* leaf_nums, int64_t n_leaves) {
+    if (nsites < 1 || nsites > (int64_t(1) << 30)) return fail(h, MCPHY_ERR_ARG, "nsites out of range");
+    if (nnodes < 3) return fail(h, MCPHY_ERR_ARG, "nnodes must be >= 3");
+    if (!leaf_nums || n_leaves < 2 || n_leaves >= nnodes)
+        return fail(h, MCPHY_ERR_ARG, "need 2 <= n_leaves < nnodes leaf nums");
+    std::vector<char> seen(nnodes, 0);
+    for (int64_t l = 0; l < n_leaves; ++l) {
+        int64_t v = leaf_nums[l];
+        if (v < 1 || v > nnodes) return fail(h, MCPHY_ERR_ARG, "leaf num out of range");
+        if (seen[v - 1]) return fail(h, MCPHY_ERR_ARG, "duplicate leaf num");
+        seen[v - 1] = 1;
+    }
+    Inst& in = h->inst[i];
+    const bool reshaped = (in.S != nsites) || (in.data_N != nnodes) ||
+                          (int64_t(in.leaf_nums.size()) != n_leaves) ||
+                          !std::equal(in.leaf_nums.begin(), in.leaf_nums.end(), leaf_nums);
+    in.S = nsites;
+    in.data_N = nnodes;
+    in.leaf_nums.assign(leaf_nums, leaf_nums + n_leaves);
+    in.has_data = true;
+    h->dirty |= DIRTY_DATA;
+    if (reshaped) h->dirty |= DIRTY_LAYOUT;
+    return MCPHY_OK;
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int mcphy_version(void) { return 100; }
+
+const char* mcphy_status_string(int s) {
+    switch (s) {
+        case MCPHY_OK: return "ok";
+        case MCPHY_ERR_ARG: return "bad argument";
+        case MCPHY_ERR_SHAPE: return "dimension mismatch";
+        case MCPHY_ERR_TREE: return "invalid tree";
+        case MCPHY_ERR_OOM: return "out of memory";
+        case MCPHY_ERR_CUDA: return "CUDA error";
+        case MCPHY_ERR_STATE: return "tree, data or model not set";
+        case MCPHY_ERR_TIMEOUT: return "device wait timed out";
+        case MCPHY_ERR_NO_DEVICE: return "no CUDA device";
+        case MCPHY_ERR_DATA: return "non-finite input";
+        default: return "unknown status";
+    }
+}
+
+const char* mcphy_last_error(mcphy_handle h) { return h ? h->err.c_str() : "null handle"; }
+
+int mcphy_batch_create(int64_t nbase, int64_t nrates, int64_t n_instances, int precision,
+                       mcphy_handle* out) {
+    if (!out) return MCPHY_ERR_ARG;
+    *out = nullptr;
+    if (nbase < 2 || nbase > 32) return MCPHY_ERR_ARG;
+    if (nrates < 1 || nrates > 64) return MCPHY_ERR_ARG;
+    if (n_instances < 1 || n_instances > 65535) return MCPHY_ERR_ARG;
+    if (precision != MCPHY_PREC_F32 && precision != MCPHY_PREC_F64) return MCPHY_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return MCPHY_ERR_NO_DEVICE;
+    }
+    mcphy_engine* h = new (std::nothrow) mcphy_engine();
+    if (!h) return MCPHY_ERR_OOM;
+    h->K = int(nbase);
+    h->Kp = kp_of(h->K);
+    h->C = int(nrates);
+    h->prec = precision;
+    h->M = n_instances;
+    h->inst.resize(size_t(n_instances));
+    if (cudaGetDevice(&h->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete h;
+        return MCPHY_ERR_CUDA;
+    }
+    h->stream = h->own;
+    for (auto& e : h->ev) cudaEventCreate(&e);
+    *out = h;
+    return MCPHY_OK;
+}
+
+int mcphy_create(int64_t nbase, int64_t nrates, int precision, mcphy_handle* out) {
+    return mcphy_batch_create(nbase, nrates, 1, precision, out);
+}
+
+int mcphy_destroy(mcphy_handle h) {
+    if (!h) return MCPHY_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    DevBuf* bufs[] = {&h->d_desc, &h->d_sched, &h->d_items, &h->d_queue, &h->d_rows, &h->d_P,
+                      &h->d_dP, &h->d_codes, &h->d_dense, &h->d_params, &h->d_blen, &h->d_pgrad,
+                      &h->d_pll, &h->d_part, &h->d_out, &h->d_post, &h->d_pre, &h->d_counter};
+    for (DevBuf* b : bufs)
+        if (b->p) cudaFree(b->p);
+    if (h->h_blen) cudaFreeHost(h->h_blen);
+    if (h->h_out) cudaFreeHost(h->h_out);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+    return MCPHY_OK;
+}
+
+int mcphy_batch_set_data(mcphy_handle h, int64_t i, const double* x, int64_t nsites,
+                         int64_t nnodes, const int64_t* leaf_nums, int64_t n_leaves) {
+    int rc;
+    if ((rc = check_instance(h, i))) return rc;
+    if (!x) return fail(h, MCPHY_ERR_ARG, "x is NULL");
+    if ((rc = set_data_common(h, i, nsites, nnodes, leaf_nums, n_leaves))) return rc;
+    Inst& in = h->inst[i];
+    const int K = h->K;
+    const bool was_dense = in.dense;
+    bool binary = true;
+    for (int64_t l = 0; l < n_leaves && binary; ++l) {
+        const double* sl = x + size_t(leaf_nums[l] - 1) * K * nsites;
+        for (int64_t e = 0; e < int64_t(K) * nsites; ++e) {
+            double v = sl[e];
+            if (!std::isfinite(v)) {
+                in.has_data = false;
+                return fail(h, MCPHY_ERR_DATA, "non-finite leaf data");
+            }
+            if (v != 0.0 && v != 1.0) { binary = false; break; }
+        }
+    }
+    in.dense = !binary;
+    if (binary) {
+        in.codes.assign(size_t(n_leaves * nsites), 0u);
+        in.dvals.clear();
+        for (int64_t l = 0; l < n_leaves; ++l) {
+            const double* sl = x + size_t(leaf_nums[l] - 1) * K * nsites;
+            for (int64_t s = 0; s < nsites; ++s) {
+                uint32_t c = 0;
+                for (int k = 0; k < K; ++k)
+                    if (sl[s * K + k] == 1.0) c |= (1u << k);
+                in.codes[l * nsites + s] = c;
+            }
+        }
+    } else {
+        in.codes.clear();
+        in.dvals.resize(size_t(n_leaves * nsites * K));
+        for (int64_t l = 0; l < n_leaves; ++l) {
+            const double* sl = x + size_t(leaf_nums[l] - 1) * K * nsites;
+            for (int64_t e = 0; e < int64_t(K) * nsites; ++e) {
+                if (!std::isfinite(sl[e])) {
+                    in.has_data = false;
+                    return fail(h, MCPHY_ERR_DATA, "non-finite leaf data");
+                }
+                in.dvals[size_t(l * nsites * K + e)] = sl[e];
+            }
+        }
+    }
+    if (in.dense != was_dense) h->dirty |= DIRTY_LAYOUT;
+    return MCPHY_OK;
+}
+
+int mcphy_set_data(mcphy_handle h, const double* x, int64_t nsites, int64_t nnodes,
+                   const int64_t* leaf_nums, int64_t n_leaves) {
+    return mcphy_batch_set_data(h, 0, x, nsites, nnodes, leaf_nums, n_leaves);
+}
+
+int mcphy_batch_set_codes(mcphy_handle h, int64_t i, const uint32_t* codes, int64_t nsites,
+                          const int64_t* leaf_nums, int64_t n_leaves) {
+    int rc;
+    if ((rc = check_instance(h, i))) return rc;
+    if (!codes) return fail(h, MCPHY_ERR_ARG, "codes is NULL");
+    // nnodes is implied by the tree: leaves < N; use the largest leaf num bound
+    Inst& in = h->inst[i];
+    int64_t nnodes = in.has_tree ? in.N : 0;
+    if (nnodes == 0) return fail(h, MCPHY_ERR_STATE, "set the tree before compact codes");
+    if ((rc = set_data_common(h, i, nsites, nnodes, leaf_nums, n_leaves))) return rc;
+    const uint32_t allmask = (h->K == 32) ? 0xffffffffu : ((1u << h->K) - 1u);
+    for (int64_t e = 0; e < n_leaves * nsites; ++e)
+        if (codes[e] & ~allmask) {
+            in.has_data = false;
+            return fail(h, MCPHY_ERR_ARG, "state bitmask has bits >= K");
+        }
+    if (in.dense) h->dirty |= DIRTY_LAYOUT;
+    in.dense = false;
+    in.dvals.clear();
+    in.codes.assign(codes, codes + n_leaves * nsites);
+    return MCPHY_OK;
+}
+
+int mcphy_batch_set_tree(mcphy_handle h, int64_t i, int64_t nnodes, const int64_t* parent,
+                         const double* blen) {
+    int rc;
+    if ((rc = check_instance(h, i))) return rc;
+    if (!parent) return fail(h, MCPHY_ERR_ARG, "parent is NULL");
+    Schedule sc;
+    std::string e = build_schedule(nnodes, parent, std::vector<int32_t>(), sc);
+    if (!e.empty()) return fail(h, MCPHY_ERR_TREE, e);
+    Inst& in = h->inst[i];
+    if (!blen && (!in.has_tree || in.N != nnodes))
+        return fail(h, MCPHY_ERR_ARG, "blen is NULL and no lengths of this size are set");
+    if (blen && !all_finite(blen, nnodes - 1)) return fail(h, MCPHY_ERR_DATA, "non-finite branch length");
+    in.N = nnodes;
+    in.parent.assign(parent, parent + nnodes);
+    if (blen) in.blen.assign(blen, blen + nnodes - 1);
+    in.has_tree = true;
+    h->dirty |= DIRTY_LAYOUT | DIRTY_BLEN;
+    return MCPHY_OK;
+}
+
+int mcphy_set_tree(mcphy_handle h, int64_t nnodes, const int64_t* parent, const double* blen) {
+    return mcphy_batch_set_tree(h, 0, nnodes, parent, blen);
+}
+
+int mcphy_batch_set_branch_lengths(mcphy_handle h, int64_t i, const double* blen) {
+    int rc;
+    if ((rc = check_instance(h, i))) return rc;
+    Inst& in = h->inst[i];
+    if (!in.has_tree) return fail(h, MCPHY_ERR_STATE, "set the tree first");
+    if (!blen) return fail(h, MCPHY_ERR_ARG, "blen is NULL");
+    if (!all_finite(blen, in.N - 1)) return fail(h, MCPHY_ERR_DATA, "non-finite branch length");
+    std::memcpy(in.blen.data(), blen, sizeof(double) * size_t(in.N - 1));
+    h->dirty |= DIRTY_BLEN;
+    return MCPHY_OK;
+}
+
+int mcphy_set_branch_lengths(mcphy_handle h, const double* blen) {
+    return mcphy_batch_set_branch_lengths(h, 0, blen);
+}
+
+int mcphy_batch_set_all_branch_lengths(mcphy_handle h, const double* blen_packed) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (!blen_packed) return fail(h, MCPHY_ERR_ARG, "blen is NULL");
+    int64_t off = 0;
+    for (int64_t i = 0; i < h->M; ++i)
+        if (!h->inst[i].has_tree) return fail(h, MCPHY_ERR_STATE, "set every tree first");
+    for (int64_t i = 0; i < h->M; ++i) {
+        Inst& in = h->inst[i];
+        if (!all_finite(blen_packed + off, in.N - 1))
+            return fail(h, MCPHY_ERR_DATA, "non-finite branch length");
+        std::memcpy(in.blen.data(), blen_packed + off, sizeof(double) * size_t(in.N - 1));
+        off += in.N - 1;
+    }
+    h->dirty |= DIRTY_BLEN;
+    return MCPHY_OK;
+}
+
+int mcphy_batch_set_model(mcphy_handle h, int64_t i, const double* U, const double* D,
+                          const double* Uinv, double mu, const double* pi, const double* rates) {
+    int rc;
+    if ((rc = check_instance(h, i))) return rc;
+    if (!U || !D || !Uinv || !pi || !rates) return fail(h, MCPHY_ERR_ARG, "NULL model array");
+    const int K = h->K, C = h->C;
+    if (!all_finite(U, K * K) || !all_finite(D, K) || !all_finite(Uinv, K * K) ||
+        !std::isfinite(mu) || !all_finite(pi, K) || !all_finite(rates, C))
+        return fail(h, MCPHY_ERR_DATA, "non-finite model parameter");
+    Inst& in = h->inst[i];
+    in.U.assign(U, U + K * K);
+    in.D.assign(D, D + K);
+    in.Uinv.assign(Uinv, Uinv + K * K);
+    in.mu = mu;
+    in.pi.assign(size_t(h->Kp), 0.0);
+    std::copy(pi, pi + K, in.pi.begin());
+    in.rates.assign(rates, rates + C);
+    in.has_model = true;
+    h->dirty |= DIRTY_MODEL;
+    return MCPHY_OK;
+}
+
+int mcphy_set_model(mcphy_handle h, const double* U, const double* D, const double* Uinv,
+                    double mu, const double* pi, const double* rates) {
+    return mcphy_batch_set_model(h, 0, U, D, Uinv, mu, pi, rates);
+}
+
+int mcphy_logpdf(mcphy_handle h, double* ll) { return eval_host(h, ll, nullptr, false); }
+
+int mcphy_logpdf_grad(mcphy_handle h, double* ll, double* grad) {
+    return eval_host(h, ll, grad, true);
+}
+
+int mcphy_batch_logpdf(mcphy_handle h, double* ll) { return eval_host(h, ll, nullptr, false); }
+
+int mcphy_batch_logpdf_grad(mcphy_handle h, double* ll, double* grad_packed) {
+    return eval_host(h, ll, grad_packed, true);
+}
+
+int mcphy_batch_grad_offsets(mcphy_handle h, int64_t* offsets) {
+    if (!h || !offsets) return MCPHY_ERR_ARG;
+    int64_t off = 0;
+    for (int64_t i = 0; i < h->M; ++i) {
+        offsets[i] = off;
+        if (!h->inst[i].has_tree) return fail(h, MCPHY_ERR_STATE, "set every tree first");
+        off += h->inst[i].N - 1;
+    }
+    offsets[h->M] = off;
+    return MCPHY_OK;
+}
+
+int mcphy_set_all_branch_lengths_device(mcphy_handle h, const double* d_blen_packed) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (!d_blen_packed) return fail(h, MCPHY_ERR_ARG, "blen is NULL");
+    int rc;
+    if ((rc = prepare(h))) return rc;
+    CK(cudaMemcpyAsync(h->d_blen.p, d_blen_packed, sizeof(double) * size_t(h->total_branch),
+                       cudaMemcpyDeviceToDevice, h->stream));
+    return MCPHY_OK;
+}
+
+int mcphy_logpdf_grad_device(mcphy_handle h, double* d_ll, double* d_grad_packed) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (!d_ll || !d_grad_packed) return fail(h, MCPHY_ERR_ARG, "NULL output");
+    int rc;
+    if ((rc = prepare(h))) return rc;
+    if ((rc = run(h, true))) return rc;
+    CK(cudaMemcpyAsync(d_ll, h->d_out.p, sizeof(double) * size_t(h->M), cudaMemcpyDeviceToDevice,
+                       h->stream));
+    CK(cudaMemcpyAsync(d_grad_packed, static_cast<double*>(h->d_out.p) + h->M,
+                       sizeof(double) * size_t(h->total_branch), cudaMemcpyDeviceToDevice, h->stream));
+    return MCPHY_OK;
+}
+
+int mcphy_logpdf_device(mcphy_handle h, double* d_ll) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (!d_ll) return fail(h, MCPHY_ERR_ARG, "NULL output");
+    int rc;
+    if ((rc = prepare(h))) return rc;
+    if ((rc = run(h, false))) return rc;
+    CK(cudaMemcpyAsync(d_ll, h->d_out.p, sizeof(double) * size_t(h->M), cudaMemcpyDeviceToDevice,
+                       h->stream));
+    return MCPHY_OK;
+}
+
+int mcphy_set_stream(mcphy_handle h, void* stream) {
+    if (!h) return MCPHY_ERR_ARG;
+    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own;
+    return MCPHY_OK;
+}
+
+int mcphy_synchronize(mcphy_handle h) {
+    if (!h) return MCPHY_ERR_ARG;
+    CK(cudaStreamSynchronize(h->stream));
+    return finish_timing(h);
+}
+
+int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (sites_per_thread != 0 && sites_per_thread != 1 && sites_per_thread != 2 &&
+        sites_per_thread != 4)
+        return fail(h, MCPHY_ERR_ARG, "sites_per_thread must be 0, 1, 2 or 4");
+    if (threads_per_block != 0 &&
+        (threads_per_block < 64 || threads_per_block > 256 || threads_per_block % 32 != 0))
+        return fail(h, MCPHY_ERR_ARG, "threads_per_block must be 0 or a multiple of 32 in [64, 256]");
+    h->spt_req = sites_per_thread;
+    h->tpb_req = threads_per_block;
+    h->dirty |= DIRTY_LAYOUT;
+    return MCPHY_OK;
+}
+
+int mcphy_enable_timing(mcphy_handle h, int on) {
+    if (!h) return MCPHY_ERR_ARG;
+    h->timing = on != 0;
+    return MCPHY_OK;
+}
+
+int mcphy_get_timing(mcphy_handle h, float* ms3) {
+    if (!h || !ms3) return MCPHY_ERR_ARG;
+    for (int k = 0; k < 3; ++k) ms3[k] = h->ms[k];
+    return MCPHY_OK;
+}
+
+int mcphy_get_counts(mcphy_handle h, int64_t* counts3) {
+    if (!h || !counts3) return MCPHY_ERR_ARG;
+    for (int k = 0; k < 3; ++k) counts3[k] = h->counts[k];
+    return MCPHY_OK;
+}
+
+int mcphy_schedule_info(int64_t nnodes, const int64_t* parent, int64_t* out5) {
+    if (!parent || !out5) return MCPHY_ERR_ARG;
+    Schedule sc;
+    std::string e = build_schedule(nnodes, parent, std::vector<int32_t>(), sc);
+    if (!e.empty()) return MCPHY_ERR_TREE;
+    out5[0] = sc.J;
+    out5[1] = sc.n_virtual;
+    out5[2] = int64_t(sc.leaves.size());
+    out5[3] = sc.max_depth;
+    out5[4] = sc.pre_slots;
+    return MCPHY_OK;
+}
+
+}  // extern "C"

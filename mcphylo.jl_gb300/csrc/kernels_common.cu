@@ -1,0 +1,92 @@
+// Transition-matrix build and the deterministic reduction.
+#include "kernels.cuh"
+
+namespace mcphy {
+
+// ---------------------------------------------------------------- reduction
+// Pass 1: grid (ceil(max_branch/32) + 1, n_inst, n_split), block (32, RY).
+// Block (bx, i, z) sums the items of instance i in split z (a contiguous item
+// range) for 32 branches; thread (tx, ty) takes every RY-th item of the range,
+// then the RY partial sums are added in ty order.  The last x-block does the
+// log-likelihood partials.  Pass 2 adds the n_split sums in z order.
+template <typename Real>
+__global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
+    __shared__ double red[RY][33];
+    const int i = blockIdx.y;
+    const InstanceDesc& d = a.inst[i];
+    const int64_t n_items = int64_t(a.C) * d.n_blocks;
+    const int64_t per = (n_items + a.n_split - 1) / a.n_split;
+    const int64_t q0 = int64_t(blockIdx.z) * per;
+    const int64_t q1 = min(n_items, q0 + per);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t stride = int64_t(a.total_branch) + gridDim.y;   // one split row
+    double* part = a.part + int64_t(blockIdx.z) * stride;
+    if (blockIdx.x == gridDim.x - 1) {
+        const int tid = ty * 32 + tx;
+        double acc = 0.0;
+        for (int64_t q = q0 + tid; q < q1; q += 32 * RY) acc += a.pll[d.item_off + q];
+        red[ty][tx] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0.0;
+            for (int y = 0; y < RY; ++y)
+                for (int x = 0; x < 32; ++x) s += red[y][x];
+            part[i] = s;
+        }
+        return;
+    }
+    if (!a.want_grad) return;
+    const int b = blockIdx.x * 32 + tx;
+    if (blockIdx.x * 32 >= d.n_branch) return;      // whole block past this instance
+    double acc = 0.0;
+    if (b < d.n_branch) {
+        const Real* pg = reinterpret_cast<const Real*>(a.pgrad) + d.pgrad_off + b;
+        for (int64_t q = q0 + ty; q < q1; q += RY) acc += double(pg[q * d.n_branch]);
+    }
+    red[ty][tx] = acc;
+    __syncthreads();
+    if (ty == 0 && b < d.n_branch) {
+        double s = 0.0;
+        for (int y = 0; y < RY; ++y) s += red[y][tx];
+        part[gridDim.y + d.grad_off + b] = s;
+    }
+}
+
+__global__ void reduce_pass2(const ReduceArgs a) {
+    const int64_t n = int64_t(a.n_inst) + (a.want_grad ? a.total_branch : 0);
+    const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int64_t stride = a.total_branch + a.n_inst;
+    double s = 0.0;
+    for (int z = 0; z < a.n_split; ++z) s += a.part[int64_t(z) * stride + e];
+    a.out[e] = s;
+}
+
+cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st) {
+    dim3 grid(unsigned((max_branch + 31) / 32 + 1), unsigned(a.n_inst), unsigned(a.n_split));
+    dim3 block(32, RY);
+    if (f64)
+        reduce_pass1<double><<<grid, block, 0, st>>>(a);
+    else
+        reduce_pass1<float><<<grid, block, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t n = int64_t(a.n_inst) + a.total_branch;
+    reduce_pass2<<<unsigned((n + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_p(bool f64, const BuildPArgs& a, cudaStream_t st) {
+    const int64_t total = int64_t(a.n_rows) * a.C * a.Kp;
+    if (total == 0) return cudaSuccess;
+    const int tpb = 128;
+    const int64_t blocks = (total + tpb - 1) / tpb;
+    if (f64)
+        build_transition_kernel<double><<<unsigned(blocks), tpb, 0, st>>>(a);
+    else
+        build_transition_kernel<float><<<unsigned(blocks), tpb, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+
+}  // namespace mcphy

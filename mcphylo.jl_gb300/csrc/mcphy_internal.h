@@ -1,0 +1,83 @@
+// Internal layout shared by the host runtime (api.cu, schedule.cpp) and the
+// kernels (kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace mcphy {
+
+// One binary internal node of the kernel schedule, in post-order (a proper DFS
+// post-order of the binarised tree).  Schedule index j is also the node's slot in
+// the per-warp post-order scratch; the root is j = J-1.
+//   op[c] >= 0 : child c is internal schedule node op[c]
+//   op[c] <  0 : child c is leaf row (-op[c]-1) of the instance's leaf table
+//   br[c]      : row of the instance's P/dP table for the branch above child c,
+//                equal to the gradient index node.num - 1; the last row (index
+//                n_branch) is the identity used for the zero-length "virtual"
+//                branches that binarise multifurcations (no gradient output)
+//   ps[c]      : pre-order stack slot where the backward sweep leaves child c's
+//                pre-order partial, or -1 (leaf child, or the child is the next
+//                step j-1 and receives it in registers)
+//   self_slot  : stack slot holding this node's own pre-order partial, or -1
+//                (root, or carried in registers from step j+1)
+struct alignas(16) SchedNode {
+    int32_t op[2];
+    int32_t br[2];
+    int32_t ps[2];
+    int32_t self_slot;
+    int32_t pad;
+};
+static_assert(sizeof(SchedNode) == 32, "SchedNode is two 16-byte words");
+
+// Per-instance descriptor, read by every warp that works on the instance.
+struct alignas(16) InstanceDesc {
+    int32_t J;           // schedule nodes (root = J-1)
+    int32_t S;           // sites
+    int32_t S_pad;       // sites rounded up to the site block of the launch
+    int32_t n_leaf;      // leaf rows
+    int32_t n_branch;    // real branches = N-1 (P/dP rows 0..n_branch-1, identity at n_branch)
+    int32_t dense;       // 1: leaf partials stored densely, 0: state bitmasks
+    int32_t n_blocks;    // S_pad / site block
+    int32_t pre_slots;   // pre-order stack depth of this instance
+    int64_t sched_off;   // into the schedule array (SchedNode units)
+    int64_t p_off;       // into the P / dP tables (Real units); rows are [branch][rate][Kp][Kp]
+    int64_t leaf_off;    // into the code table (code units) or dense table (Real units)
+    int64_t param_off;   // into the FP64 parameter block
+    int64_t item_off;    // first work item of this instance
+    int64_t pgrad_off;   // into the per-item gradient partials (float units)
+    int64_t blen_off;    // into the packed branch-length vector
+    int64_t grad_off;    // into the packed gradient output
+};
+
+// FP64 model parameters of one instance, packed at param_off:
+//   U (K*K, column-major) | D (K) | Uinv (K*K) | mu (1) | rates (C) | pi (Kp)
+inline int64_t param_size(int K, int Kp, int C) { return 2 * K * K + K + 1 + C + Kp; }
+
+enum DirtyBits : unsigned {
+    DIRTY_LAYOUT = 1u,   // schedule/offsets/buffer sizes changed
+    DIRTY_DATA = 2u,     // leaf tables changed
+    DIRTY_BLEN = 4u,     // branch lengths changed
+    DIRTY_MODEL = 8u,    // eigensystem / pi / rates changed
+};
+
+// Result of turning a parent array into a kernel schedule.
+struct Schedule {
+    int64_t N = 0;
+    int32_t J = 0;                 // binary internal schedule nodes
+    int32_t n_virtual = 0;         // identity branches added for multifurcations
+    int32_t max_depth = 0;
+    int32_t pre_slots = 0;         // depth of the pre-order partial stack
+    std::vector<SchedNode> nodes;  // post-order, root last
+    std::vector<int64_t> leaves;   // leaf nums in the order the schedule expects (sorted)
+};
+
+// Builds the schedule.  leaf_row_of_num maps a leaf num (1-based) to its row in
+// the leaf table (-1 if the num is not a leaf of the data); pass an empty vector
+// to only validate.  Returns an empty string on success, else the error message.
+std::string build_schedule(int64_t N, const int64_t* parent,
+                           const std::vector<int32_t>& leaf_row_of_num, Schedule& out);
+
+}  // namespace mcphy

@@ -1,0 +1,158 @@
+// Tree -> kernel schedule.
+//
+// The reference walks post_order(tree) and, for every internal node, combines all
+// of its children (comb_sum_product_loop!, src/Likelihood/VectorizedFunctions.jl:187-213;
+// FelsensteinFunction, src/Likelihood/LikelihoodCalculator_Node.jl:82-114), then
+// walks the same list backwards for the gradient (LikelihoodCalculator_Node.jl:25-74).
+//
+// The kernel wants a fixed two-operand step, so a node with m > 2 children is
+// binarised into a left-leaning chain of m-1 binary steps joined by zero-length
+// "virtual" branches (P = I, dP = 0, no gradient output): step k combines the
+// running product with child k+1 and is emitted right after child k+1's subtree,
+// so the schedule is a proper depth-first post-order of the binarised tree.  The
+// product of the children's contributions, hence logL and every real branch's
+// gradient, is unchanged; only extra power-of-two rescalings are inserted.
+//
+// Because the order is depth-first, the backward sweep (reverse order) consumes
+// stored pre-order partials last-in first-out, so they live in a small stack of
+// slots whose depth is bounded by the tree height.
+//
+// Children are taken in increasing num order; the reference takes node.children
+// order.  The two only differ in the order of a product, i.e. in rounding.
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "mcphy_internal.h"
+
+namespace mcphy {
+
+std::string build_schedule(int64_t N, const int64_t* parent,
+                           const std::vector<int32_t>& leaf_row_of_num, Schedule& out) {
+    out = Schedule();
+    if (N < 3) return "a tree needs at least 3 nodes (root and two children)";
+    if (N > (int64_t(1) << 30)) return "too many nodes";
+    if (parent == nullptr) return "parent array is NULL";
+    if (parent[N - 1] != 0) return "the root must be node N (parent[N-1] == 0)";
+
+    // children lists, CSR, in increasing num order
+    std::vector<int64_t> cnt(N + 1, 0);
+    for (int64_t i = 0; i < N - 1; ++i) {
+        int64_t p = parent[i];
+        if (p == 0) return "more than one root (parent == 0 at num " + std::to_string(i + 1) + ")";
+        if (p < 1 || p > N) return "parent of num " + std::to_string(i + 1) + " out of range";
+        if (p == i + 1) return "node " + std::to_string(i + 1) + " is its own parent";
+        cnt[p]++;
+    }
+    std::vector<int64_t> cptr(N + 1, 0);
+    for (int64_t n = 1; n <= N; ++n) cptr[n] = cptr[n - 1] + cnt[n];
+    std::vector<int64_t> cidx(std::max<int64_t>(cptr[N], 1));
+    std::vector<int64_t> fill(cptr.begin(), cptr.end() - 1);
+    for (int64_t i = 0; i < N - 1; ++i) cidx[fill[parent[i] - 1]++] = i + 1;
+
+    for (int64_t n = 1; n <= N; ++n)
+        if (cptr[n] - cptr[n - 1] == 1)
+            return "node " + std::to_string(n) + " has a single child (unary nodes are not supported)";
+
+    const bool map_leaves = !leaf_row_of_num.empty();
+    if (map_leaves && (int64_t)leaf_row_of_num.size() < N) return "leaf map shorter than N";
+
+    // operand of a finished child: leaf row or its schedule index
+    std::vector<int32_t> sched_id(N, -1);
+    std::string err;
+    auto operand = [&](int64_t c) -> int32_t {
+        if (cptr[c] - cptr[c - 1] == 0) {
+            int32_t row = map_leaves ? leaf_row_of_num[c - 1] : 0;
+            if (row < 0) err = "leaf " + std::to_string(c) + " has no data row";
+            return -row - 1;
+        }
+        return sched_id[c - 1];
+    };
+
+    struct Frame {
+        int64_t num;
+        int64_t next;     // next child to visit
+        int32_t acc_op;   // running binary product so far
+        int32_t acc_br;
+    };
+    std::vector<Frame> st;
+    std::vector<int32_t> depth(N, 0);
+    st.push_back({N, 0, 0, 0});
+    int64_t visited = 0;
+    int32_t max_depth = 0;
+    const int32_t ident = int32_t(N - 1);   // identity row of the P table
+    out.nodes.reserve(size_t(N));
+
+    while (!st.empty()) {
+        Frame& f = st.back();
+        const int64_t n = f.num;
+        const int64_t nch = cptr[n] - cptr[n - 1];
+        if (f.next < nch) {
+            const int64_t c = cidx[cptr[n - 1] + f.next];
+            depth[c - 1] = depth[n - 1] + 1;
+            max_depth = std::max(max_depth, depth[c - 1]);
+            st.push_back({c, 0, 0, 0});
+            continue;
+        }
+        // node n is finished
+        st.pop_back();
+        if (++visited > N) return "cycle in parent array";
+        if (nch == 0) out.leaves.push_back(n);
+        else sched_id[n - 1] = int32_t(out.nodes.size()) - 1;
+        if (st.empty()) break;
+        // fold child n into its parent's running product
+        Frame& pf = st.back();
+        const int64_t pn = pf.num;
+        const int64_t pnch = cptr[pn] - cptr[pn - 1];
+        const int32_t opn = operand(n);
+        if (!err.empty()) return err;
+        if (pf.next == 0) {
+            pf.acc_op = opn;
+            pf.acc_br = int32_t(n - 1);
+        } else {
+            SchedNode sn{};
+            sn.op[0] = pf.acc_op;
+            sn.br[0] = pf.acc_br;
+            sn.op[1] = opn;
+            sn.br[1] = int32_t(n - 1);
+            sn.ps[0] = sn.ps[1] = -1;
+            sn.self_slot = -1;
+            sn.pad = 0;
+            out.nodes.push_back(sn);
+            pf.acc_op = int32_t(out.nodes.size()) - 1;
+            pf.acc_br = ident;
+            if (pf.next < pnch - 1) out.n_virtual++;
+        }
+        pf.next++;
+    }
+    if (visited != N) return "parent array is not connected to the root (cycle or forest)";
+    out.N = N;
+    out.J = int32_t(out.nodes.size());
+    out.max_depth = max_depth;
+    std::sort(out.leaves.begin(), out.leaves.end());
+
+    // Pre-order stack slots.  The backward sweep runs j = J-1 .. 0; at step j the
+    // pre-order partial of each internal child goes to registers if the child is
+    // step j-1, else onto the stack; it is popped when the child's step runs.
+    std::vector<int32_t> slot_of(out.J, -1);
+    int32_t top = 0, max_top = 0;
+    for (int32_t j = out.J - 1; j >= 0; --j) {
+        SchedNode& sn = out.nodes[j];
+        if (slot_of[j] >= 0) {
+            if (slot_of[j] != top - 1) return "internal error: pre-order stack is not LIFO";
+            sn.self_slot = slot_of[j];
+            --top;
+        }
+        for (int c = 0; c < 2; ++c) {
+            const int32_t o = sn.op[c];
+            if (o < 0 || o == j - 1) continue;
+            sn.ps[c] = top;
+            slot_of[o] = top++;
+            max_top = std::max(max_top, top);
+        }
+    }
+    out.pre_slots = std::max(max_top, 1);
+    return std::string();
+}
+
+}  // namespace mcphy

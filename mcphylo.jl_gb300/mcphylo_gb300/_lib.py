@@ -1,0 +1,119 @@
+"""ctypes binding of libmcphylo_gpu.so (declared in include/mcphylo_gpu.h).
+
+The library is built in-tree by ``mcphylo.jl_gb300/build.py``.  There is no CPU
+fallback: if the shared library is missing, or no CUDA device is visible, the
+calls raise instead of computing anything on the host.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmcphylo_gpu.so")
+
+OK = 0
+ERR_ARG, ERR_SHAPE, ERR_TREE, ERR_OOM, ERR_CUDA, ERR_STATE, ERR_TIMEOUT, ERR_NO_DEVICE, ERR_DATA = (
+    -1, -2, -3, -4, -5, -6, -7, -8, -9)
+PREC_F32 = 0
+PREC_F64 = 1
+
+i64 = ctypes.c_int64
+c_int = ctypes.c_int
+dbl = ctypes.c_double
+P = ctypes.POINTER
+pdbl = P(dbl)
+pi64 = P(i64)
+pu32 = P(ctypes.c_uint32)
+handle_t = ctypes.c_void_p
+
+# name -> (restype, argtypes); exactly the functions include/mcphylo_gpu.h declares
+SIGNATURES = {
+    "mcphy_create": (c_int, [i64, i64, c_int, P(handle_t)]),
+    "mcphy_destroy": (c_int, [handle_t]),
+    "mcphy_set_data": (c_int, [handle_t, pdbl, i64, i64, pi64, i64]),
+    "mcphy_set_tree": (c_int, [handle_t, i64, pi64, pdbl]),
+    "mcphy_set_branch_lengths": (c_int, [handle_t, pdbl]),
+    "mcphy_set_model": (c_int, [handle_t, pdbl, pdbl, pdbl, dbl, pdbl, pdbl]),
+    "mcphy_logpdf": (c_int, [handle_t, pdbl]),
+    "mcphy_logpdf_grad": (c_int, [handle_t, pdbl, pdbl]),
+    "mcphy_batch_create": (c_int, [i64, i64, i64, c_int, P(handle_t)]),
+    "mcphy_batch_set_data": (c_int, [handle_t, i64, pdbl, i64, i64, pi64, i64]),
+    "mcphy_batch_set_codes": (c_int, [handle_t, i64, pu32, i64, pi64, i64]),
+    "mcphy_batch_set_tree": (c_int, [handle_t, i64, i64, pi64, pdbl]),
+    "mcphy_batch_set_branch_lengths": (c_int, [handle_t, i64, pdbl]),
+    "mcphy_batch_set_all_branch_lengths": (c_int, [handle_t, pdbl]),
+    "mcphy_batch_set_model": (c_int, [handle_t, i64, pdbl, pdbl, pdbl, dbl, pdbl, pdbl]),
+    "mcphy_batch_logpdf": (c_int, [handle_t, pdbl]),
+    "mcphy_batch_logpdf_grad": (c_int, [handle_t, pdbl, pdbl]),
+    "mcphy_batch_grad_offsets": (c_int, [handle_t, pi64]),
+    "mcphy_set_all_branch_lengths_device": (c_int, [handle_t, ctypes.c_void_p]),
+    "mcphy_logpdf_grad_device": (c_int, [handle_t, ctypes.c_void_p, ctypes.c_void_p]),
+    "mcphy_logpdf_device": (c_int, [handle_t, ctypes.c_void_p]),
+    "mcphy_set_stream": (c_int, [handle_t, ctypes.c_void_p]),
+    "mcphy_synchronize": (c_int, [handle_t]),
+    "mcphy_set_tiles": (c_int, [handle_t, c_int, c_int]),
+    "mcphy_enable_timing": (c_int, [handle_t, c_int]),
+    "mcphy_get_timing": (c_int, [handle_t, P(ctypes.c_float)]),
+    "mcphy_get_counts": (c_int, [handle_t, pi64]),
+    "mcphy_last_error": (ctypes.c_char_p, [handle_t]),
+    "mcphy_status_string": (ctypes.c_char_p, [c_int]),
+    "mcphy_version": (c_int, []),
+    "mcphy_schedule_info": (c_int, [i64, pi64, pi64]),
+}
+
+_lib = None
+
+
+class MCPhyError(RuntimeError):
+    """A non-zero status from the engine."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+class DimensionMismatch(MCPhyError, ValueError):
+    """Sizes disagree (the reference throws DimensionMismatch, Phylodist.jl:195-217)."""
+
+
+class NoDeviceError(MCPhyError):
+    """No CUDA device: the engine has no CPU fallback."""
+
+
+def load():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with `python mcphylo.jl_gb300/build.py` "
+            "(there is no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int, h=None, what: str = "") -> None:
+    if status == OK:
+        return
+    L = load()
+    msg = ""
+    if h is not None:
+        msg = (L.mcphy_last_error(h) or b"").decode()
+    if not msg:
+        msg = (L.mcphy_status_string(status) or b"").decode()
+    if what:
+        msg = f"{what}: {msg}"
+    if status == ERR_SHAPE:
+        raise DimensionMismatch(status, msg)
+    if status == ERR_NO_DEVICE:
+        raise NoDeviceError(status, msg)
+    if status in (ERR_ARG, ERR_TREE, ERR_DATA):
+        raise ValueError(f"{msg} (status {status})")
+    raise MCPhyError(status, msg)

@@ -1,0 +1,198 @@
+"""Python side of the engine: a thin owner of one libmcphylo_gpu handle.
+
+``Engine`` is the object a sampler keeps for a whole chain: the data is uploaded
+once, and each leapfrog step only sends the branch lengths and reads back the
+log-likelihood and gradient.  ``Engine(..., n_instances=M)`` is the batched form
+(MultiplePhyloDist): M independent trees, data sets and models in one launch.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+_PREC = {"f32": _lib.PREC_F32, "fp32": _lib.PREC_F32, "float32": _lib.PREC_F32,
+         "f64": _lib.PREC_F64, "fp64": _lib.PREC_F64, "float64": _lib.PREC_F64}
+
+
+def _pd(a: np.ndarray):
+    return a.ctypes.data_as(_lib.pdbl)
+
+
+def _pi64(a: np.ndarray):
+    return a.ctypes.data_as(_lib.pi64)
+
+
+def _f64(a, order="C") -> np.ndarray:
+    return np.require(np.asarray(a, dtype=np.float64), requirements=[order[0], "A"])
+
+
+class Engine:
+    """Owner of one engine handle (K states, C rate categories, M instances)."""
+
+    def __init__(self, nbase: int, nrates: int, precision: str = "f32", n_instances: int = 1):
+        L = _lib.load()
+        self._L = L
+        self.K = int(nbase)
+        self.C = int(nrates)
+        self.M = int(n_instances)
+        self.precision = precision
+        h = _lib.handle_t()
+        st = L.mcphy_batch_create(self.K, self.C, self.M, _PREC[precision], ctypes.byref(h))
+        if st != _lib.OK:
+            check(st, None, "mcphy_batch_create")
+        self._h = h
+        self._N = [0] * self.M
+        self._grad_off = None
+
+    # ------------------------------------------------------------------ lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.mcphy_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------------ setters
+    def set_data(self, x: np.ndarray, leaf_nums: Sequence[int], i: int = 0) -> None:
+        """x: the reference's (K, S, N) FP64 tensor; leaf slices at x[:, :, num-1]."""
+        x = np.asfortranarray(x, dtype=np.float64)
+        if x.ndim != 3 or x.shape[0] != self.K:
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, f"x must be ({self.K}, S, N), got {x.shape}")
+        ln = np.ascontiguousarray(leaf_nums, dtype=np.int64)
+        check(self._L.mcphy_batch_set_data(self._h, i, _pd(x), x.shape[1], x.shape[2], _pi64(ln),
+                                           len(ln)), self._h, "set_data")
+
+    def set_codes(self, codes: np.ndarray, leaf_nums: Sequence[int], i: int = 0) -> None:
+        """codes: (n_leaves, S) uint32 state bitmasks, row l for leaf leaf_nums[l]."""
+        c = np.ascontiguousarray(codes, dtype=np.uint32)
+        ln = np.ascontiguousarray(leaf_nums, dtype=np.int64)
+        if c.ndim != 2 or c.shape[0] != len(ln):
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, "codes must be (n_leaves, S)")
+        check(self._L.mcphy_batch_set_codes(self._h, i, c.ctypes.data_as(_lib.pu32), c.shape[1],
+                                            _pi64(ln), len(ln)), self._h, "set_codes")
+
+    def set_tree(self, parent: Sequence[int], blen: Optional[Sequence[float]] = None,
+                 i: int = 0) -> None:
+        p = np.ascontiguousarray(parent, dtype=np.int64)
+        b = None if blen is None else np.ascontiguousarray(blen, dtype=np.float64)
+        if b is not None and len(b) != len(p) - 1:
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, "blen must have N-1 entries")
+        check(self._L.mcphy_batch_set_tree(self._h, i, len(p), _pi64(p),
+                                           None if b is None else _pd(b)), self._h, "set_tree")
+        self._N[i] = len(p)
+        self._grad_off = None
+
+    def set_branch_lengths(self, blen, i: int = 0) -> None:
+        b = np.ascontiguousarray(blen, dtype=np.float64)
+        if len(b) != self._N[i] - 1:
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, "blen must have N-1 entries")
+        check(self._L.mcphy_batch_set_branch_lengths(self._h, i, _pd(b)), self._h,
+              "set_branch_lengths")
+
+    def set_all_branch_lengths(self, blen_packed) -> None:
+        b = np.ascontiguousarray(blen_packed, dtype=np.float64)
+        if len(b) != sum(self._N) - self.M:
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, "packed blen has the wrong length")
+        check(self._L.mcphy_batch_set_all_branch_lengths(self._h, _pd(b)), self._h,
+              "set_all_branch_lengths")
+
+    def set_model(self, U, D, Uinv, mu: float, pi, rates, i: int = 0) -> None:
+        if np.iscomplexobj(U) or np.iscomplexobj(D) or np.iscomplexobj(Uinv):
+            raise ValueError("the likelihood path needs a real eigensystem")
+        Uf = np.asfortranarray(U, dtype=np.float64)
+        Uif = np.asfortranarray(Uinv, dtype=np.float64)
+        Dd = np.ascontiguousarray(D, dtype=np.float64)
+        pid = np.ascontiguousarray(pi, dtype=np.float64)
+        rd = np.ascontiguousarray(rates, dtype=np.float64)
+        if Uf.shape != (self.K, self.K) or Uif.shape != (self.K, self.K) or len(Dd) != self.K \
+                or len(pid) != self.K:
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, "model arrays do not match K")
+        if len(rd) != self.C:
+            raise _lib.DimensionMismatch(_lib.ERR_SHAPE, "rates do not match C")
+        check(self._L.mcphy_batch_set_model(self._h, i, _pd(Uf), _pd(Dd), _pd(Uif), float(mu),
+                                            _pd(pid), _pd(rd)), self._h, "set_model")
+
+    def set_tiles(self, sites_per_thread: int = 0, threads_per_block: int = 0) -> None:
+        check(self._L.mcphy_set_tiles(self._h, sites_per_thread, threads_per_block), self._h,
+              "set_tiles")
+
+    def set_stream(self, stream_ptr: int) -> None:
+        check(self._L.mcphy_set_stream(self._h, ctypes.c_void_p(stream_ptr or None)), self._h)
+
+    def enable_timing(self, on: bool = True) -> None:
+        check(self._L.mcphy_enable_timing(self._h, 1 if on else 0), self._h)
+
+    # ------------------------------------------------------------------ evaluation
+    def grad_offsets(self) -> np.ndarray:
+        if self._grad_off is None:
+            off = np.zeros(self.M + 1, dtype=np.int64)
+            check(self._L.mcphy_batch_grad_offsets(self._h, _pi64(off)), self._h)
+            self._grad_off = off
+        return self._grad_off
+
+    def logpdf(self):
+        ll = np.zeros(self.M, dtype=np.float64)
+        check(self._L.mcphy_batch_logpdf(self._h, _pd(ll)), self._h, "logpdf")
+        return float(ll[0]) if self.M == 1 else ll
+
+    def logpdf_grad(self, out_ll: Optional[np.ndarray] = None,
+                    out_grad: Optional[np.ndarray] = None):
+        """-> (ll, grad) for one instance, (ll[M], packed grad) for a batch."""
+        off = self.grad_offsets()
+        ll = out_ll if out_ll is not None else np.zeros(self.M, dtype=np.float64)
+        g = out_grad if out_grad is not None else np.zeros(int(off[-1]), dtype=np.float64)
+        check(self._L.mcphy_batch_logpdf_grad(self._h, _pd(ll), _pd(g)), self._h, "logpdf_grad")
+        if self.M == 1:
+            return float(ll[0]), g
+        return ll, g
+
+    def logpdf_grad_device(self, d_ll_ptr: int, d_grad_ptr: int) -> None:
+        check(self._L.mcphy_logpdf_grad_device(self._h, ctypes.c_void_p(d_ll_ptr),
+                                               ctypes.c_void_p(d_grad_ptr)), self._h)
+
+    def logpdf_device(self, d_ll_ptr: int) -> None:
+        check(self._L.mcphy_logpdf_device(self._h, ctypes.c_void_p(d_ll_ptr)), self._h)
+
+    def set_all_branch_lengths_device(self, d_blen_ptr: int) -> None:
+        check(self._L.mcphy_set_all_branch_lengths_device(self._h, ctypes.c_void_p(d_blen_ptr)),
+              self._h)
+
+    def synchronize(self) -> None:
+        check(self._L.mcphy_synchronize(self._h), self._h)
+
+    def timing(self):
+        ms = (ctypes.c_float * 3)()
+        check(self._L.mcphy_get_timing(self._h, ms), self._h)
+        return {"build_p_ms": ms[0], "prune_ms": ms[1], "reduce_ms": ms[2]}
+
+    def counts(self):
+        c = np.zeros(3, dtype=np.int64)
+        check(self._L.mcphy_get_counts(self._h, _pi64(c)), self._h)
+        return {"launches": int(c[0]), "units": int(c[1]), "scratch_bytes": int(c[2])}
+
+
+def schedule_info(parent) -> dict:
+    """Host-only: validate a parent array and describe its kernel schedule."""
+    L = _lib.load()
+    p = np.ascontiguousarray(parent, dtype=np.int64)
+    out = np.zeros(5, dtype=np.int64)
+    st = L.mcphy_schedule_info(len(p), _pi64(p), _pi64(out))
+    if st != _lib.OK:
+        raise ValueError("invalid tree (parent array)")
+    return {"internal": int(out[0]), "virtual": int(out[1]), "leaves": int(out[2]),
+            "max_depth": int(out[3]), "pre_slots": int(out[4])}

@@ -1,0 +1,97 @@
+"""Shared helpers for the GPU parity tests: random problems and the oracle call."""
+import numpy as np
+
+from oracle import pyoracle as O
+
+import mcphylo_gb300 as mp
+from mcphylo_gb300 import models, simulate
+from mcphylo_gb300.tree import Node, number_nodes, post_order, to_parent
+
+
+def collapse(tree: Node, rng, p: float) -> Node:
+    """Merge a fraction p of internal edges into their parents (multifurcations)."""
+    for n in list(post_order(tree)):
+        if n.mother is not None and n.children and rng.random() < p:
+            m = n.mother
+            i = m.children.index(n)
+            kids = n.children
+            for k in kids:
+                k.mother = m
+                k.inc_length += 0.0
+            m.children[i:i + 1] = kids
+    number_nodes(tree)
+    return tree
+
+
+def caterpillar(n_taxa: int, rng, mean=0.1) -> Node:
+    root = Node()
+    cur = root
+    for i in range(n_taxa - 1):
+        a = cur.add_child(Node(f"t{i}"))
+        a.inc_length = rng.exponential(mean)
+        if i < n_taxa - 2:
+            nxt = cur.add_child(Node())
+        else:
+            nxt = cur.add_child(Node(f"t{i + 1}"))
+        nxt.inc_length = rng.exponential(mean)
+        cur = nxt
+    number_nodes(root)
+    return root
+
+
+def random_instance(K, C, taxa, S, seed, multifurcate=0.0, missing=0.05, tree=None,
+                    model="gtr"):
+    rng = np.random.default_rng(seed)
+    if tree is None:
+        tree = simulate.yule_tree(taxa, rng, 0.15)
+        if multifurcate:
+            tree = collapse(tree, rng, multifurcate)
+    pi = rng.dirichlet(np.full(K, 4.0))
+    if model == "restriction" and K == 2:
+        m = models.Restriction(pi)
+    elif model == "jc":
+        pi = np.ones(K) / K
+        m = models.JC(pi)
+    else:
+        m = models.GTR(pi, rng.dirichlet(np.ones(K * (K - 1) // 2)) * K)
+    rates = models.discrete_gamma_rates(0.7, 0.7, C) if C > 1 else np.array([1.0])
+    return simulate._instance(tree, m, pi, rates, S, rng, missing)
+
+
+def oracle(inst, blen=None):
+    t = O.tree_from_parent(inst.parent, inst.blen if blen is None else blen)
+    return O.gradlogpdf(t, inst.tensor(), inst.pi, (inst.U, inst.D, inst.Uinv, inst.mu),
+                        inst.rates)
+
+
+def oracle_ll(inst, blen=None):
+    t = O.tree_from_parent(inst.parent, inst.blen if blen is None else blen)
+    return O.logpdf(t, inst.tensor(), inst.pi, (inst.U, inst.D, inst.Uinv, inst.mu), inst.rates)
+
+
+def engine(inst, precision, spt=0, dense=False):
+    e = mp.Engine(inst.K, len(inst.rates), precision)
+    if spt:
+        e.set_tiles(spt, 0)
+    e.set_tree(inst.parent, inst.blen)
+    if dense:
+        e.set_data(inst.tensor(), inst.leaf_nums)
+    else:
+        e.set_codes(inst.codes, inst.leaf_nums)
+    e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    return e
+
+
+# Tolerances (the benchmark spec): plain FP64 path within 1e-12 relative of the oracle; the
+# FP32-scaled path within 1e-6 relative on logL and 1e-4 relative per gradient entry.
+# Gradient entries are compared relative to max(|g_i|, floor * max_j |g_j|): an entry
+# that cancels to nearly zero is held to the scale of the vector it belongs to.
+F64_RTOL, F32_LL_RTOL, F32_G_RTOL = 1e-12, 1e-6, 1e-4
+
+
+def assert_grad_close(g, go, rtol, floor):
+    g, go = np.asarray(g), np.asarray(go)
+    scale = np.maximum(np.abs(go), floor * np.max(np.abs(go)))
+    err = np.abs(g - go) / scale
+    assert np.all(err <= rtol), (float(err.max()), int(err.argmax()))
+    return float(err.max())

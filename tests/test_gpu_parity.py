@@ -1,0 +1,221 @@
+"""CUDA path (through the C ABI) against the CPU oracle and the reference's goldens."""
+import numpy as np
+import pytest
+
+from conftest import load_alignment
+from gpu_cases import (F32_G_RTOL, F32_LL_RTOL, F64_RTOL, assert_grad_close, caterpillar,
+                       engine, oracle, oracle_ll, random_instance)
+
+import mcphylo_gb300 as mp
+from mcphylo_gb300 import parse, simulate, tree as T
+
+pytestmark = pytest.mark.gpu
+
+
+def _golden_pd(golden, name, precision):
+    key = "primates" if name == "primates" else "simudata"
+    g = golden["felsenstein"][key]
+    a = load_alignment(name)
+    t = T.parse_newick(g["newick"])
+    syms = parse.get_alphabet(a["rows"], "-", "?")
+    x = parse.datafortree(a["rows"], a["taxa"], t, syms, "-", "?")
+    pden = np.ones(4) / 4
+    return mp.PhyloDist(t, pden, [1.0], [1.0], mp.JC, precision=precision), x, g
+
+
+@pytest.mark.parametrize("precision,rtol", [("f64", F64_RTOL), ("f32", F32_LL_RTOL)])
+def test_primates_golden(built_lib, golden, precision, rtol):
+    pd, x, g = _golden_pd(golden, "primates", precision)
+    ll = mp.logpdf(pd, x)
+    assert abs(ll - g["logpdf"]) <= rtol * abs(g["logpdf"])
+
+
+@pytest.mark.parametrize("precision,rtol", [("f64", F64_RTOL), ("f32", F32_G_RTOL)])
+def test_simudata_gradient_golden(built_lib, golden, precision, rtol):
+    pd, x, g = _golden_pd(golden, "simudata", precision)
+    ll, grad = mp.gradlogpdf(pd, x)
+    assert_grad_close(grad, g["grad"], rtol, 1e-3)
+    # the reference's own ll golden is only good to its isapprox tolerance
+    assert abs(ll - g["ll"]) <= 1.5e-8 * abs(g["ll"])
+
+
+def test_multiplephylodist_golden(built_lib, golden):
+    pd, x, g = _golden_pd(golden, "primates", "f64")
+    mpd = mp.MultiplePhyloDist([pd.tree, pd.tree], np.full((4, 2), 0.25), [1.0], [1.0], mp.JC)
+    x4 = np.stack([x, x], axis=3)
+    assert abs(mp.logpdf(mpd, x4) - 2 * g["logpdf"]) <= 1e-12 * abs(2 * g["logpdf"])
+    res = mp.phylodist.__logpdf(mpd, x4)
+    for ll, grad in res:
+        assert abs(ll - g["logpdf"]) <= 1e-12 * abs(g["logpdf"])
+        assert grad.shape == (21,)
+
+
+CASES = [
+    # K, C, taxa, S, multifurcate, model
+    (2, 1, 3, 1, 0.0, "restriction"),
+    (2, 1, 32, 1000, 0.0, "restriction"),
+    (2, 4, 40, 257, 0.0, "restriction"),
+    (3, 2, 17, 33, 0.3, "gtr"),
+    (4, 1, 25, 100, 0.0, "jc"),
+    (4, 4, 60, 513, 0.2, "gtr"),
+    (5, 3, 12, 31, 0.0, "gtr"),
+    (8, 2, 20, 64, 0.0, "gtr"),
+    (20, 4, 16, 40, 0.0, "gtr"),
+]
+
+
+@pytest.mark.parametrize("K,C,taxa,S,mf,model", CASES)
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_random_vs_oracle(built_lib, K, C, taxa, S, mf, model, precision):
+    inst = random_instance(K, C, taxa, S, seed=K * 100 + C * 10 + taxa, multifurcate=mf,
+                           model=model)
+    llo, go = oracle(inst)
+    for spt in ((1, 2, 4) if K <= 4 else (1,)):
+        if precision == "f64" and spt == 4:
+            continue
+        e = engine(inst, precision, spt)
+        ll, g = e.logpdf_grad()
+        assert e.logpdf() == pytest.approx(ll, rel=1e-15, abs=0)
+        if precision == "f64":
+            assert abs(ll - llo) <= F64_RTOL * abs(llo), (ll, llo)
+            assert_grad_close(g, go, F64_RTOL * 10, 1e-3)
+        else:
+            assert abs(ll - llo) <= F32_LL_RTOL * abs(llo), (ll, llo)
+            assert_grad_close(g, go, F32_G_RTOL, 1e-2)
+        e.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_dense_leaf_values(built_lib, precision):
+    """Leaf partials that are not 0/1 (ambiguity weights) take the dense path."""
+    inst = random_instance(4, 2, 15, 70, seed=7)
+    x = inst.tensor()
+    rng = np.random.default_rng(3)
+    for n in inst.leaf_nums:
+        x[:, :, n - 1] = x[:, :, n - 1] * 0.8 + 0.2 * rng.random((4, inst.S))
+    from oracle import pyoracle as O
+    t = O.tree_from_parent(inst.parent, inst.blen)
+    llo, go = O.gradlogpdf(t, x, inst.pi, (inst.U, inst.D, inst.Uinv, inst.mu), inst.rates)
+    e = mp.Engine(4, 2, precision)
+    e.set_tree(inst.parent, inst.blen)
+    e.set_data(x, inst.leaf_nums)
+    e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    ll, g = e.logpdf_grad()
+    tol = F64_RTOL if precision == "f64" else F32_LL_RTOL
+    assert abs(ll - llo) <= tol * abs(llo)
+    assert_grad_close(g, go, F64_RTOL * 10 if precision == "f64" else F32_G_RTOL, 1e-2)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_deep_caterpillar(built_lib, precision):
+    rng = np.random.default_rng(11)
+    inst = random_instance(4, 2, 0, 96, seed=11, tree=caterpillar(150, rng))
+    llo, go = oracle(inst)
+    ll, g = engine(inst, precision).logpdf_grad()
+    tol = F64_RTOL if precision == "f64" else F32_LL_RTOL
+    assert abs(ll - llo) <= tol * abs(llo)
+    assert_grad_close(g, go, F64_RTOL * 10 if precision == "f64" else F32_G_RTOL, 1e-2)
+
+
+def test_gradient_matches_central_fd(built_lib):
+    inst = random_instance(4, 4, 20, 200, seed=5)
+    e = engine(inst, "f64")
+    ll, g = e.logpdf_grad()
+    h = 1e-6
+    for i in range(0, inst.N - 1, 3):
+        b = inst.blen.copy()
+        b[i] += h
+        e.set_branch_lengths(b)
+        lp = e.logpdf()
+        b[i] -= 2 * h
+        e.set_branch_lengths(b)
+        lm = e.logpdf()
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd, g[i])
+
+
+def test_branch_lengths_and_topology_updates(built_lib):
+    inst = random_instance(4, 2, 30, 150, seed=9)
+    e = engine(inst, "f64")
+    rng = np.random.default_rng(0)
+    b2 = inst.blen * rng.uniform(0.5, 1.5, size=inst.blen.shape)
+    e.set_branch_lengths(b2)
+    ll, g = e.logpdf_grad()
+    llo, go = oracle(inst, b2)
+    assert abs(ll - llo) <= F64_RTOL * abs(llo)
+    # NNI-like move: swap a leaf with its parent's sibling subtree; nums are kept
+    parent = inst.parent.copy()
+    leaf = int(inst.leaf_nums[0])
+    p = parent[leaf - 1]
+    gp = parent[p - 1]
+    if gp == 0:
+        leaf = int(inst.leaf_nums[-1])
+        p = parent[leaf - 1]
+        gp = parent[p - 1]
+    sib = [i + 1 for i in range(len(parent)) if parent[i] == gp and i + 1 != p][0]
+    parent[leaf - 1], parent[sib - 1] = gp, p
+    e.set_tree(parent, b2)
+    ll, g = e.logpdf_grad()
+    inst2 = simulate.Instance(T.from_parent(parent, b2), parent, b2, inst.leaf_nums, inst.codes,
+                              inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    llo, go = oracle(inst2)
+    assert abs(ll - llo) <= F64_RTOL * abs(llo)
+    assert_grad_close(g, go, F64_RTOL * 10, 1e-3)
+
+
+def test_batched_uneven_instances(built_lib):
+    batch = simulate.hky_batch(seed=8, n=6, taxa=(5, 120), sites=(1, 3000), scale=1.0)
+    for precision in ("f64", "f32"):
+        e = mp.Engine(4, 4, precision, n_instances=len(batch))
+        for i, b in enumerate(batch):
+            e.set_tree(b.parent, b.blen, i)
+            e.set_codes(b.codes, b.leaf_nums, i)
+            e.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, i)
+        ll, g = e.logpdf_grad()
+        off = e.grad_offsets()
+        for i, b in enumerate(batch):
+            llo, go = oracle(b)
+            if precision == "f64":
+                assert abs(ll[i] - llo) <= F64_RTOL * abs(llo)
+                assert_grad_close(g[off[i]:off[i + 1]], go, F64_RTOL * 10, 1e-3)
+            else:
+                assert abs(ll[i] - llo) <= F32_LL_RTOL * abs(llo)
+                assert_grad_close(g[off[i]:off[i + 1]], go, F32_G_RTOL, 1e-2)
+        e.close()
+
+
+def test_deterministic_and_site_additive(built_lib):
+    """Same inputs -> bitwise-identical results; logL and gradient are sums over
+    sites, so two halves add up to the whole."""
+    inst = random_instance(4, 4, 50, 3000, seed=21)
+    e = engine(inst, "f64")
+    a = e.logpdf_grad()
+    b = e.logpdf_grad()
+    assert a[0] == b[0] and np.array_equal(a[1], b[1])
+    h = inst.S // 2
+    parts = []
+    for sl in (slice(0, h), slice(h, inst.S)):
+        e2 = mp.Engine(4, 4, "f64")
+        e2.set_tree(inst.parent, inst.blen)
+        e2.set_codes(inst.codes[:, sl], inst.leaf_nums)
+        e2.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+        parts.append(e2.logpdf_grad())
+    assert abs(parts[0][0] + parts[1][0] - a[0]) <= 1e-12 * abs(a[0])
+    np.testing.assert_allclose(parts[0][1] + parts[1][1], a[1], rtol=1e-10,
+                               atol=1e-10 * np.abs(a[1]).max())
+
+
+def test_full_size_gtr_gamma_f32_vs_f64(built_lib):
+    """GTR+G4, 128 taxa, 100,000 sites: FP32-scaled path within 1e-6 (logL) and
+    1e-4 (gradient entries) of the plain FP64 GPU path at full size."""
+    inst = simulate.gtr_gamma(S=100_000, with_weights=False)
+    ll64, g64 = engine(inst, "f64").logpdf_grad()
+    ll32, g32 = engine(inst, "f32").logpdf_grad()
+    assert abs(ll32 - ll64) <= F32_LL_RTOL * abs(ll64)
+    assert_grad_close(g32, g64, F32_G_RTOL, 1e-2)
+    # the oracle on a 2,000-site slice ties the FP64 path to the reference loops
+    sub = simulate.Instance(inst.tree, inst.parent, inst.blen, inst.leaf_nums, inst.codes[:, :2000],
+                            inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    llo, go = oracle(sub)
+    ll, g = engine(sub, "f64").logpdf_grad()
+    assert abs(ll - llo) <= F64_RTOL * abs(llo)

@@ -1,0 +1,122 @@
+"""The oracle (oracle/) against the reference's own golden values.
+
+Tolerances: the reference's tests use Julia's isapprox (rtol = sqrt(eps) ~ 1.5e-8);
+the oracle restates the same FP64 loops, so it is held to 1e-12 where the golden
+is itself tight (primates logL, the simudata gradient).  The simudata ll golden
+agrees with every FP64 evaluation to 1.95e-9 only, i.e. within the reference
+test's own 1.5e-8 tolerance, so that one entry is checked at 1.5e-8.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_alignment
+from oracle import pyoracle as O
+
+RTOL_JULIA = float(np.sqrt(np.finfo(float).eps))
+
+
+def _case(name, newick):
+    a = load_alignment(name)
+    tree = O.parse_newick(newick)
+    symbols = sorted(set("".join(a["rows"])) - {"-", "?"})
+    x = O.datafortree(a["rows"], a["taxa"], tree, symbols, "-", "?")
+    return tree, x
+
+
+def test_primates_logpdf(golden):
+    g = golden["felsenstein"]["primates"]
+    tree, x = _case("primates", g["newick"])
+    pi = np.ones(4) / 4
+    ll = O.logpdf(tree, x, pi, O.JC(pi), [1.0])
+    assert abs(ll - g["logpdf"]) <= 1e-12 * abs(g["logpdf"])
+
+
+def test_simudata_gradient_pins_numbering(golden):
+    g = golden["felsenstein"]["simudata"]
+    tree, x = _case("simudata", g["newick"])
+    pi = np.ones(4) / 4
+    ll, grad = O.gradlogpdf(tree, x, pi, O.JC(pi), [1.0])
+    gold = np.array(g["grad"])
+    assert grad.shape == gold.shape == (17,)
+    np.testing.assert_allclose(grad, gold, rtol=1e-12)
+    assert abs(ll - g["ll"]) <= RTOL_JULIA * abs(g["ll"])
+
+
+def test_oracle_gradient_matches_central_fd(golden):
+    g = golden["felsenstein"]["simudata"]
+    tree, x = _case("simudata", g["newick"])
+    pi = np.ones(4) / 4
+    m = O.JC(pi)
+    _, grad = O.gradlogpdf(tree, x, pi, m, [1.0])
+    blv = O.flatten(tree)[6]
+    h = 1e-6
+    for i in range(len(blv)):
+        bp, bm = blv.copy(), blv.copy()
+        bp[i] += h
+        bm[i] -= h
+        fd = (O.logpdf(tree, x, pi, m, [1.0], bp) - O.logpdf(tree, x, pi, m, [1.0], bm)) / (2 * h)
+        assert abs(fd - grad[i]) <= 1e-6 * max(1.0, abs(grad[i]))
+
+
+def test_multiplephylodist_is_sum(golden):
+    """test/distributions/phylodist.jl:133-135: two copies give 2x the golden."""
+    g = golden["felsenstein"]["primates"]
+    tree, x = _case("primates", g["newick"])
+    pi = np.ones(4) / 4
+    tot = sum(O.logpdf(tree, x, pi, O.JC(pi), [1.0]) for _ in range(2))
+    assert abs(tot - 2 * g["logpdf"]) <= 1e-12 * abs(2 * g["logpdf"])
+
+
+def test_models(golden):
+    sm = golden["substitution_models"]
+    r = sm["restriction"]
+    U, D, Uinv, mu = O.Restriction(r["base_freq"])
+    np.testing.assert_allclose(U, r["U"], rtol=RTOL_JULIA)
+    np.testing.assert_allclose(D, r["D"], rtol=RTOL_JULIA)
+    np.testing.assert_allclose(Uinv, r["Uinv"], rtol=1e-8)
+    assert abs(mu - r["mu"]) <= RTOL_JULIA * r["mu"]
+    with pytest.raises(AssertionError):
+        O.Restriction(np.ones(3) / 3)
+    j = sm["jc"]
+    U, D, Uinv, mu = O.JC(j["base_freq"])
+    np.testing.assert_allclose(U @ np.diag(D) @ Uinv, j["Q"], atol=1e-12)
+    assert abs(mu - j["mu"]) < 1e-12
+    for key, fn, args in (("gtr", O.GTR, lambda m: (m["base_freq"], m["rates"])),
+                          ("freek", O.freeK, lambda m: ([0.0], m["rates"]))):
+        m = sm[key]
+        U, D, Uinv, mu = fn(*args(m))
+        np.testing.assert_allclose(D, m["D"], rtol=RTOL_JULIA, atol=1e-15)
+        # eigenvectors up to sign: compare P(t) = U exp(D t) Uinv instead
+        Ug, Dg, Uig = np.array(m["U"]), np.array(m["D"]), np.array(m["Uinv"])
+        for t in (0.01, 0.3, 2.0):
+            P = U @ np.diag(np.exp(D * t)) @ Uinv
+            Pg = Ug @ np.diag(np.exp(Dg * t)) @ Uig
+            np.testing.assert_allclose(P, Pg, atol=1e-12)
+        assert abs(mu - m["mu"]) <= 1e-12 * m["mu"]
+    s = sm["setmatrix"]
+    np.testing.assert_array_equal(O.setmatrix(s["input"]), np.array(s["output"]))
+
+
+def test_rates(golden):
+    """The reference computes the mean-method CDF with gamma_inc(a, x, 1), i.e.
+    SpecialFunctions' reduced-accuracy mode (about 6 significant digits,
+    src/Likelihood/Rates.jl:23); scipy's gammainc is full precision, so the mean
+    rates agree to ~3e-9, inside the reference test's own isapprox tolerance."""
+    r = golden["rates"]
+    np.testing.assert_allclose(O.discrete_gamma_rates(r["alpha"], r["beta"], r["k"]), r["mean"],
+                               rtol=RTOL_JULIA)
+    np.testing.assert_allclose(O.discrete_gamma_rates(r["alpha"], r["beta"], r["k"], "median"),
+                               r["median"], rtol=1e-12)
+    np.testing.assert_allclose(O.median_boundaries(r["alpha"], r["beta"], r["k"]),
+                               r["median_boundaries"], rtol=1e-12)
+    np.testing.assert_allclose(O.mean_boundaries(r["alpha"], r["beta"], r["k"])[:3],
+                               r["mean_boundaries"], rtol=1e-12)
+
+
+def test_oracle_transition_matrices_are_stochastic():
+    rng = np.random.default_rng(0)
+    pi = rng.dirichlet(np.ones(4) * 5)
+    m = O.GTR(pi, rng.dirichlet(np.ones(6)))
+    P, dP = O.transition_matrices(m, [0.3, 1.7], rng.exponential(0.2, size=7))
+    np.testing.assert_allclose(P.sum(axis=1), 1.0, atol=1e-12)
+    np.testing.assert_allclose(dP.sum(axis=1), 0.0, atol=1e-12)
