@@ -158,32 +158,42 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- CPU sample
-def cpu_sample(insts, seconds, max_sites=2000):
+def cpu_sample(insts, seconds, window=2000):
     """The oracle (FP64 restatement of the reference loops, OpenMP over all host
-    cores) on the workload's instances in order, each truncated to its first
-    max_sites sites, until ``seconds`` have elapsed."""
+    cores) on the workload itself: instance by instance, window of ``window``
+    sites by window, until ``seconds`` of oracle time have been spent.  Only the
+    oracle's logL + gradient call is timed."""
     from oracle import pyoracle as O
     from mcphylo_gb300 import simulate
     O.lib()
     units = 0
-    done = 0
-    t0 = time.perf_counter()
-    for b in insts:
-        S = min(b.S, max_sites)
-        sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums, b.codes[:, :S], b.U, b.D,
-                                b.Uinv, b.mu, b.pi, b.rates)
-        x = sub.tensor()
-        t = O.tree_from_parent(sub.parent, sub.blen)
-        ts = time.perf_counter()
-        O.gradlogpdf(t, x, sub.pi, (sub.U, sub.D, sub.Uinv, sub.mu), sub.rates)
-        units += sub.units()
-        done += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-        _ = ts
-    el = time.perf_counter() - t0
-    return units / el, {"instances": done, "max_sites": max_sites, "units": units,
-                        "seconds": round(el, 3), "threads": O.num_threads()}
+    calls = 0
+    spent = 0.0
+    insts_used = set()
+    done = False
+    while not done:
+        for ii, b in enumerate(insts):
+            for s0 in range(0, b.S, window):
+                sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums,
+                                        b.codes[:, s0:s0 + window], b.U, b.D, b.Uinv, b.mu,
+                                        b.pi, b.rates)
+                x = sub.tensor()
+                t = O.tree_from_parent(sub.parent, sub.blen)
+                ts = time.perf_counter()
+                O.gradlogpdf(t, x, sub.pi, (sub.U, sub.D, sub.Uinv, sub.mu), sub.rates)
+                spent += time.perf_counter() - ts
+                units += sub.units()
+                calls += 1
+                insts_used.add(ii)
+                if spent >= seconds:
+                    done = True
+                    break
+                if len(insts) > 1:
+                    break          # batched workload: one window per instance, spread out
+            if done:
+                break
+    return units / spent, {"instances": len(insts_used), "window": window, "calls": calls,
+                           "units": units, "seconds": round(spent, 3), "threads": O.num_threads()}
 
 
 # ----------------------------------------------------------------------------- reference arm
@@ -281,7 +291,9 @@ def run_gpu(args, rank, world):
     M = len(insts)
     off = e.grad_offsets()
     G = int(off[-1])
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream shared by the engine, the L2 flush and the events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     e.set_stream(stream.cuda_stream)
     e.enable_timing(True)
 
@@ -326,6 +338,7 @@ def run_gpu(args, rank, world):
         wall = time.perf_counter() - wall0
     clocks = clk.summary()
     step_ms = [s.elapsed_time(t) for s, t in zip(starts, ends)]
+    assert min(step_ms) >= 0.9 * statistics.mean(prune_ms), "events did not bracket the step"
     ms = statistics.mean(step_ms)
     if dist is not None:
         tt = torch.tensor([ms], device="cuda")
@@ -394,17 +407,22 @@ def run_gpu(args, rank, world):
     alg = algorithmic_bytes(insts, tiles[0], real_b)
     pr = statistics.mean(prune_ms)
     achieved = alg / (pr / 1e3) / 1e9
+    # DRAM bytes of one prune launch from the committed ncu capture: bytes per unit
+    # of the captured workload times this launch's units (traffic grows with units)
     traffic = None
+    traffic_note = None
     tpath = os.path.join(ROOT, "profiles", "prune_traffic.json")
     if os.path.exists(tpath):
         try:
             tj = json.load(open(tpath))
-            if tj.get("workload") == cfg["workload"]:
-                traffic = tj.get("bytes_per_launch")
+            if tj.get("kernel") == "prune_kernel<4,float,%d>" % tiles[0] and insts[0].K == 4:
+                traffic = float(tj["bytes_per_unit"]) * units
+                traffic_note = (f"ncu dram bytes of a {tj['captured_workload']} launch scaled by "
+                                f"units ({tj['bytes_per_unit']} B/unit)")
         except Exception:
             traffic = None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": traffic,
+                "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_note,
                 "kernel": "prune_kernel<4,float,%d>" % tiles[0],
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg,
@@ -415,8 +433,9 @@ def run_gpu(args, rank, world):
     if rank == 0 and not args.no_cpu:
         v, info = cpu_sample(insts, args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
-               "sample": f"oracle on {info['instances']} instances, first <={info['max_sites']} "
-                         f"sites each, {info['units']} units in {info['seconds']} s"}
+               "sample": f"oracle (FP64, OpenMP) on {info['calls']} windows of <={info['window']} "
+                         f"sites from {info['instances']} of the workload's instances, "
+                         f"{info['units']} units in {info['seconds']} s of oracle time"}
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",

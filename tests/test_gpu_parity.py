@@ -3,8 +3,9 @@ import numpy as np
 import pytest
 
 from conftest import load_alignment
-from gpu_cases import (F32_G_RTOL, F32_LL_RTOL, F64_RTOL, assert_grad_close, caterpillar,
-                       engine, oracle, oracle_ll, random_instance)
+from gpu_cases import (F32_G_FLOOR, F32_G_RTOL, F32_LL_RTOL, F64_G_FLOOR, F64_G_RTOL, F64_RTOL,
+                       assert_grad_close, caterpillar, engine, oracle, oracle_ll,
+                       random_instance)
 
 import mcphylo_gb300 as mp
 from mcphylo_gb300 import parse, simulate, tree as T
@@ -30,11 +31,14 @@ def test_primates_golden(built_lib, golden, precision, rtol):
     assert abs(ll - g["logpdf"]) <= rtol * abs(g["logpdf"])
 
 
-@pytest.mark.parametrize("precision,rtol", [("f64", F64_RTOL), ("f32", F32_G_RTOL)])
-def test_simudata_gradient_golden(built_lib, golden, precision, rtol):
+@pytest.mark.parametrize("precision,rtol,floor", [("f64", F64_RTOL, 1e-3),
+                                                   ("f32", F32_G_RTOL, F32_G_FLOOR)])
+def test_simudata_gradient_golden(built_lib, golden, precision, rtol, floor):
+    """The 17 golden entries of test/likelihood/felsenstein.jl:37; the FP64 path
+    meets them per entry (relative to max(|g_i|, 1e-3 max|g|)) at 1e-12."""
     pd, x, g = _golden_pd(golden, "simudata", precision)
     ll, grad = mp.gradlogpdf(pd, x)
-    assert_grad_close(grad, g["grad"], rtol, 1e-3)
+    assert_grad_close(grad, g["grad"], rtol, floor)
     # the reference's own ll golden is only good to its isapprox tolerance
     assert abs(ll - g["ll"]) <= 1.5e-8 * abs(g["ll"])
 
@@ -78,10 +82,10 @@ def test_random_vs_oracle(built_lib, K, C, taxa, S, mf, model, precision):
         assert e.logpdf() == pytest.approx(ll, rel=1e-15, abs=0)
         if precision == "f64":
             assert abs(ll - llo) <= F64_RTOL * abs(llo), (ll, llo)
-            assert_grad_close(g, go, F64_RTOL * 10, 1e-3)
+            assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
         else:
             assert abs(ll - llo) <= F32_LL_RTOL * abs(llo), (ll, llo)
-            assert_grad_close(g, go, F32_G_RTOL, 1e-2)
+            assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
         e.close()
 
 
@@ -103,7 +107,10 @@ def test_dense_leaf_values(built_lib, precision):
     ll, g = e.logpdf_grad()
     tol = F64_RTOL if precision == "f64" else F32_LL_RTOL
     assert abs(ll - llo) <= tol * abs(llo)
-    assert_grad_close(g, go, F64_RTOL * 10 if precision == "f64" else F32_G_RTOL, 1e-2)
+    if precision == "f64":
+        assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
+    else:
+        assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
@@ -114,7 +121,10 @@ def test_deep_caterpillar(built_lib, precision):
     ll, g = engine(inst, precision).logpdf_grad()
     tol = F64_RTOL if precision == "f64" else F32_LL_RTOL
     assert abs(ll - llo) <= tol * abs(llo)
-    assert_grad_close(g, go, F64_RTOL * 10 if precision == "f64" else F32_G_RTOL, 1e-2)
+    if precision == "f64":
+        assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
+    else:
+        assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
 
 
 def test_gradient_matches_central_fd(built_lib):
@@ -160,7 +170,7 @@ def test_branch_lengths_and_topology_updates(built_lib):
                               inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
     llo, go = oracle(inst2)
     assert abs(ll - llo) <= F64_RTOL * abs(llo)
-    assert_grad_close(g, go, F64_RTOL * 10, 1e-3)
+    assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
 
 
 def test_batched_uneven_instances(built_lib):
@@ -177,10 +187,10 @@ def test_batched_uneven_instances(built_lib):
             llo, go = oracle(b)
             if precision == "f64":
                 assert abs(ll[i] - llo) <= F64_RTOL * abs(llo)
-                assert_grad_close(g[off[i]:off[i + 1]], go, F64_RTOL * 10, 1e-3)
+                assert_grad_close(g[off[i]:off[i + 1]], go, F64_G_RTOL, F64_G_FLOOR)
             else:
                 assert abs(ll[i] - llo) <= F32_LL_RTOL * abs(llo)
-                assert_grad_close(g[off[i]:off[i + 1]], go, F32_G_RTOL, 1e-2)
+                assert_grad_close(g[off[i]:off[i + 1]], go, F32_G_RTOL, F32_G_FLOOR)
         e.close()
 
 
@@ -212,7 +222,7 @@ def test_full_size_gtr_gamma_f32_vs_f64(built_lib):
     ll64, g64 = engine(inst, "f64").logpdf_grad()
     ll32, g32 = engine(inst, "f32").logpdf_grad()
     assert abs(ll32 - ll64) <= F32_LL_RTOL * abs(ll64)
-    assert_grad_close(g32, g64, F32_G_RTOL, 1e-2)
+    assert_grad_close(g32, g64, F32_G_RTOL, F32_G_FLOOR)
     # the oracle on a 2,000-site slice ties the FP64 path to the reference loops
     sub = simulate.Instance(inst.tree, inst.parent, inst.blen, inst.leaf_nums, inst.codes[:, :2000],
                             inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
