@@ -134,6 +134,23 @@ int mcphy_set_all_branch_lengths_device(mcphy_handle h, const double* d_blen_pac
 int mcphy_logpdf_grad_device(mcphy_handle h, double* d_ll, double* d_grad_packed);
 int mcphy_logpdf_device(mcphy_handle h, double* d_ll);
 
+/* ------------------------------------------------------------------ allocation-free call
+ * No counterpart in the reference: an extension for callers that cannot allocate
+ * device memory while they evaluate (cudaMalloc synchronises the whole device and
+ * may be forbidden inside their loop or outside their own memory budget).  Same
+ * result as mcphy_batch_logpdf_grad for the branch lengths in d_blen_packed (device
+ * memory, packed by instance), written to d_ll[M] and d_grad_packed (device
+ * memory), asynchronously on the handle's stream.  It allocates nothing: its
+ * scratch is one fixed 64 MiB device array inside the library, shared by every
+ * call in the process (calls whose GPU work overlaps race; serialise them); only
+ * the work counter in it is cleared per call.  Problems whose per-item partial
+ * sums exceed the array are rejected with MCPHY_ERR_ARG.  Tree, data and model
+ * must have been uploaded by a regular evaluation since they last changed
+ * (MCPHY_ERR_STATE otherwise).  The first call on a device looks up the array's
+ * device address; make it before any stream capture. */
+int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_packed, double* d_ll,
+                              double* d_grad_packed);
+
 /* ------------------------------------------------------------------ control
  * Stream: run on the caller's stream (a cudaStream_t cast to void*); NULL restores
  * the handle's own stream. */

@@ -1,0 +1,92 @@
+// Internal state of an engine handle (struct mcphy_engine), shared by the
+// translation units that implement the C ABI.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mcphy_internal.h"
+
+namespace mcphy {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct Inst {
+    // tree
+    int64_t N = 0;
+    std::vector<int64_t> parent;
+    std::vector<double> blen;
+    bool has_tree = false;
+    // data
+    int64_t S = 0;
+    int64_t data_N = 0;
+    std::vector<int64_t> leaf_nums;
+    bool dense = false;
+    std::vector<uint32_t> codes;   // [leaf_row][S]
+    std::vector<double> dvals;     // [leaf_row][S][K]
+    bool has_data = false;
+    // model
+    std::vector<double> U, D, Uinv, pi, rates;
+    double mu = 0.0;
+    bool has_model = false;
+};
+
+}  // namespace mcphy
+
+
+struct mcphy_engine {
+    using DevBuf = mcphy::DevBuf;
+    using Inst = mcphy::Inst;
+    using InstanceDesc = mcphy::InstanceDesc;
+    using SchedNode = mcphy::SchedNode;
+    int K = 0, Kp = 0, C = 0, prec = 0;
+    int64_t M = 0;
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<Inst> inst;
+    unsigned dirty = mcphy::DIRTY_LAYOUT | mcphy::DIRTY_DATA | mcphy::DIRTY_BLEN | mcphy::DIRTY_MODEL;
+
+    // launch shape
+    int spt_req = 0, tpb_req = 0;
+    int spt = 1, tpb = 256, blocks = 0;
+
+    // layout
+    std::vector<InstanceDesc> desc;
+    std::vector<int64_t> grad_offsets;   // M + 1
+    int64_t total_branch = 0;
+    int64_t n_items = 0;
+    int64_t n_prows = 0;
+    int32_t max_J = 0;
+    int32_t max_branch = 0;
+    int64_t units = 0;
+    int64_t warp_stride = 0;
+    int64_t pre_warp_stride = 0;
+    int32_t max_pre = 0;
+    int64_t leaf_elems = 0;
+    bool any_dense = false;
+    std::vector<SchedNode> sched_all;
+
+    DevBuf d_desc, d_sched, d_items, d_queue, d_rows, d_P, d_dP, d_codes, d_dense, d_params,
+        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter;
+    int n_split = 1;
+
+    double* h_blen = nullptr;
+    size_t h_blen_cap = 0;
+    double* h_out = nullptr;
+    size_t h_out_cap = 0;
+
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float ms[3] = {0.f, 0.f, 0.f};
+    int64_t counts[3] = {0, 0, 0};
+    std::string err;
+};
+

@@ -50,6 +50,8 @@ SIGNATURES = {
     "mcphy_set_all_branch_lengths_device": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_logpdf_grad_device": (c_int, [handle_t, ctypes.c_void_p, ctypes.c_void_p]),
     "mcphy_logpdf_device": (c_int, [handle_t, ctypes.c_void_p]),
+    "mcphy_logpdf_grad_noalloc": (c_int, [handle_t, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
     "mcphy_set_stream": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_synchronize": (c_int, [handle_t]),
     "mcphy_set_tiles": (c_int, [handle_t, c_int, c_int]),
