@@ -105,7 +105,12 @@ void choose_tiles(mcphy_engine* h) {
     else if (h->Kp > 8) spt = 1;
     if (spt != 1 && spt != 2 && spt != 4) spt = 1;
     h->spt = spt;
-    h->tpb = h->tpb_req ? h->tpb_req : 256;
+    int tpb = h->tpb_req ? h->tpb_req : 128;
+    // every warp owns two staging buffers of step records in shared memory
+    const int per_warp = warp_smem_bytes(h->Kp, spt, int(real_size(h)));
+    const int max_warps = std::max(1, (200 * 1024) / per_warp);
+    while (tpb / 32 > max_warps && tpb > 32) tpb -= 32;
+    h->tpb = tpb;
 }
 
 // Rebuilds schedules, offsets, work items and device tables.
@@ -122,8 +127,9 @@ int layout(mcphy_engine* h) {
     h->units = 0;
     h->any_dense = false;
 
-    int64_t sched_off = 0, p_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
-            pgrad_off = 0, blen_off = 0, nrows = 0;
+    const int64_t rbytes = rec_bytes(Kp, int(real_size(h)));
+    int64_t sched_off = 0, rec_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
+            pgrad_off = 0, blen_off = 0, nsteps = 0;
     const int64_t psize = param_size(K, Kp, C);
     for (int64_t i = 0; i < h->M; ++i) {
         Inst& in = h->inst[i];
@@ -151,7 +157,7 @@ int layout(mcphy_engine* h) {
         d.dense = in.dense ? 1 : 0;
         d.pre_slots = sc.pre_slots;
         d.sched_off = sched_off;
-        d.p_off = p_off;
+        d.rec_off = rec_off;
         d.leaf_off = leaf_off;
         d.param_off = param_off;
         d.item_off = item_off;
@@ -160,14 +166,16 @@ int layout(mcphy_engine* h) {
         d.grad_off = blen_off;
         h->sched_all.insert(h->sched_all.end(), sc.nodes.begin(), sc.nodes.end());
         sched_off += sc.J;
-        p_off += int64_t(d.n_branch + 1) * C * Kp * Kp;
-        leaf_off += int64_t(d.n_leaf) * d.S_pad * (in.dense ? Kp : 1);
+        rec_off += int64_t(C) * sc.J * rbytes;
+        // code leaves: the leaf codes arranged in schedule order, [block][step][operand][32*spt]
+        // (internal operands leave their entries unused); dense leaves: [row][S_pad][Kp]
+        leaf_off += in.dense ? int64_t(d.n_leaf) * d.S_pad * Kp : int64_t(sc.J) * 2 * d.S_pad;
         param_off += psize;
         const int64_t items = int64_t(C) * d.n_blocks;
         item_off += items;
         pgrad_off += items * d.n_branch;
         blen_off += d.n_branch;
-        nrows += d.n_branch + 1;
+        nsteps += sc.J;
         h->grad_offsets[i + 1] = blen_off;
         h->max_J = std::max(h->max_J, sc.J);
         h->max_pre = std::max(h->max_pre, sc.pre_slots);
@@ -177,19 +185,20 @@ int layout(mcphy_engine* h) {
     }
     h->total_branch = blen_off;
     h->n_items = item_off;
-    h->n_prows = nrows;
+    h->n_steps = nsteps;
+    h->rec_bytes_total = rec_off;
     h->leaf_elems = leaf_off;
     if (h->n_items >= (int64_t(1) << 31)) return fail(h, MCPHY_ERR_ARG, "too many work items");
 
     // work items and the order warps take them: largest trees first
     std::vector<int2> items(h->n_items);
-    std::vector<int2> rows(nrows);
-    int64_t rr = 0;
+    std::vector<int2> steps(nsteps);
+    int64_t ss = 0;
     for (int64_t i = 0; i < h->M; ++i) {
         const InstanceDesc& d = h->desc[i];
         for (int64_t q = 0; q < int64_t(C) * d.n_blocks; ++q)
             items[d.item_off + q] = make_int2(int(i), int(q));
-        for (int b = 0; b <= d.n_branch; ++b) rows[rr++] = make_int2(int(i), b);
+        for (int j = 0; j < d.J; ++j) steps[ss++] = make_int2(int(i), j);
     }
     std::vector<int64_t> order(h->M);
     std::iota(order.begin(), order.end(), 0);
@@ -208,9 +217,8 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_sched, sizeof(SchedNode) * h->sched_all.size()))) return rc;
     if ((rc = ensure(h, h->d_items, sizeof(int2) * items.size()))) return rc;
     if ((rc = ensure(h, h->d_queue, sizeof(int32_t) * queue.size()))) return rc;
-    if ((rc = ensure(h, h->d_rows, sizeof(int2) * rows.size()))) return rc;
-    if ((rc = ensure(h, h->d_P, rs * size_t(p_off)))) return rc;
-    if ((rc = ensure(h, h->d_dP, rs * size_t(p_off)))) return rc;
+    if ((rc = ensure(h, h->d_steps, sizeof(int2) * steps.size()))) return rc;
+    if ((rc = ensure(h, h->d_recs, size_t(rec_off)))) return rc;
     if ((rc = ensure(h, h->d_params, sizeof(double) * size_t(param_off)))) return rc;
     if ((rc = ensure(h, h->d_blen, sizeof(double) * size_t(h->total_branch)))) return rc;
     if ((rc = ensure(h, h->d_pgrad, rs * size_t(pgrad_off)))) return rc;
@@ -234,7 +242,7 @@ int layout(mcphy_engine* h) {
                   cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_items.p, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_queue.p, queue.data(), sizeof(int32_t) * queue.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(h->d_rows.p, rows.data(), sizeof(int2) * rows.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_steps.p, steps.data(), sizeof(int2) * steps.size(), cudaMemcpyHostToDevice));
 
     // persistent grid: as many resident warps as the SMs hold, never more than items
     int bps = 0;
@@ -268,6 +276,7 @@ int upload_data(mcphy_engine* h) {
     const int K = h->K, Kp = h->Kp;
     const uint32_t allmask = (K == 32) ? 0xffffffffu : ((1u << K) - 1u);
     const bool f64 = h->prec == MCPHY_PREC_F64;
+    const int SB = 32 * h->spt;
     std::vector<uint8_t> c8;
     std::vector<uint32_t> c32;
     std::vector<float> df;
@@ -278,22 +287,44 @@ int upload_data(mcphy_engine* h) {
     }
     for (int64_t i = 0; i < h->M; ++i) {
         const Inst& in = h->inst[i];
-        const InstanceDesc& d = h->desc[i];
-        for (int64_t l = 0; l < d.n_leaf; ++l) {
-            for (int64_t s = 0; s < d.S_pad; ++s) {
-                if (!in.dense) {
-                    uint32_t c = (s < in.S) ? in.codes[l * in.S + s] : allmask;
-                    const int64_t o = d.leaf_off + l * d.S_pad + s;
-                    if (Kp <= 8) c8[o] = uint8_t(c); else c32[o] = c;
-                } else {
+        InstanceDesc& d = h->desc[i];
+        // a code that is neither one state nor all states (or none) needs the
+        // kernel's general bitmask path for this instance
+        d.ambig = 0;
+        if (!in.dense)
+            for (uint32_t c : in.codes)
+                if (c != allmask && (c == 0u || (c & (c - 1u)) != 0u)) {
+                    d.ambig = 1;
+                    break;
+                }
+        if (in.dense) {
+            for (int64_t l = 0; l < d.n_leaf; ++l)
+                for (int64_t s = 0; s < d.S_pad; ++s) {
                     const int64_t o = d.leaf_off + (l * d.S_pad + s) * Kp;
                     for (int k = 0; k < K; ++k) {
                         double v = (s < in.S) ? in.dvals[(l * in.S + s) * K + k] : 1.0;
                         if (f64) dd[o + k] = v; else df[o + k] = float(v);
                     }
                 }
-            }
+            continue;
         }
+        // leaf codes in schedule order: entry (block, step j, operand c) holds the
+        // codes of the block's sites for the leaf that is operand c of step j
+        const SchedNode* sn = h->sched_all.data() + d.sched_off;
+        for (int j = 0; j < d.J; ++j)
+            for (int c = 0; c < 2; ++c) {
+                if (sn[j].op[c] >= 0) continue;
+                const int64_t row = -int64_t(sn[j].op[c]) - 1;
+                const uint32_t* src = in.codes.data() + row * in.S;
+                for (int64_t b = 0; b < d.n_blocks; ++b) {
+                    const int64_t o = d.leaf_off + ((b * d.J + j) * 2 + c) * SB;
+                    for (int t = 0; t < SB; ++t) {
+                        const int64_t s = b * SB + t;
+                        const uint32_t v = (s < in.S) ? src[s] : allmask;
+                        if (Kp <= 8) c8[o + t] = uint8_t(v); else c32[o + t] = v;
+                    }
+                }
+            }
     }
     if (Kp <= 8) CK(cudaMemcpy(h->d_codes.p, c8.data(), c8.size(), cudaMemcpyHostToDevice));
     else CK(cudaMemcpy(h->d_codes.p, c32.data(), c32.size() * 4, cudaMemcpyHostToDevice));
@@ -301,6 +332,7 @@ int upload_data(mcphy_engine* h) {
         if (f64) CK(cudaMemcpy(h->d_dense.p, dd.data(), dd.size() * 8, cudaMemcpyHostToDevice));
         else CK(cudaMemcpy(h->d_dense.p, df.data(), df.size() * 4, cudaMemcpyHostToDevice));
     }
+    CK(cudaMemcpy(h->d_desc.p, h->desc.data(), sizeof(InstanceDesc) * h->M, cudaMemcpyHostToDevice));
     h->dirty &= ~unsigned(DIRTY_DATA);
     return MCPHY_OK;
 }
@@ -362,31 +394,28 @@ int run(mcphy_engine* h, bool want_grad) {
     cudaStream_t st = h->stream;
     if (h->timing) CK(cudaEventRecord(h->ev[0], st));
 
-    BuildPArgs b{};
+    BuildRecArgs b{};
     b.inst = static_cast<const InstanceDesc*>(h->d_desc.p);
-    b.rows = static_cast<const int2*>(h->d_rows.p);
-    b.n_rows = int32_t(h->n_prows);
+    b.sched = static_cast<const SchedNode*>(h->d_sched.p);
+    b.steps = static_cast<const int2*>(h->d_steps.p);
+    b.n_steps = int32_t(h->n_steps);
     b.params = static_cast<const double*>(h->d_params.p);
     b.blen = static_cast<const double*>(h->d_blen.p);
-    b.P = h->d_P.p;
-    b.dP = h->d_dP.p;
+    b.recs = static_cast<unsigned char*>(h->d_recs.p);
     b.K = h->K;
     b.Kp = h->Kp;
     b.C = h->C;
-    b.want_grad = want_grad ? 1 : 0;
-    CK(launch_build_p(f64, b, st));
+    CK(launch_build_records(f64, b, st));
     if (h->timing) CK(cudaEventRecord(h->ev[1], st));
 
-    CK(cudaMemsetAsync(h->d_counter.p, 0, sizeof(int32_t), st));
+    CK(cudaMemsetAsync(h->d_counter.p, 0, 2 * sizeof(int32_t), st));
     PruneArgs a{};
     a.inst = b.inst;
-    a.sched = static_cast<const SchedNode*>(h->d_sched.p);
     a.items = static_cast<const int2*>(h->d_items.p);
     a.queue = static_cast<const int32_t*>(h->d_queue.p);
     a.n_items = int32_t(h->n_items);
     a.counter = static_cast<int32_t*>(h->d_counter.p);
-    a.P = h->d_P.p;
-    a.dP = h->d_dP.p;
+    a.recs = b.recs;
     a.codes = h->d_codes.p;
     a.dense = h->d_dense.p;
     a.params = b.params;
@@ -416,7 +445,7 @@ int run(mcphy_engine* h, bool want_grad) {
     r.out = static_cast<double*>(h->d_out.p);
     CK(launch_reduce(f64, r, h->max_branch, st));
     if (h->timing) CK(cudaEventRecord(h->ev[3], st));
-    h->counts[0] = 4;   // build_transition, prune, reduce_pass1, reduce_pass2
+    h->counts[0] = 4;   // build_records, prune, reduce_pass1, reduce_pass2
     h->counts[1] = h->units;
     return MCPHY_OK;
 }
@@ -437,7 +466,11 @@ int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
     if ((rc = run(h, want_grad))) return rc;
     const size_t n = size_t(h->M) + (want_grad ? size_t(h->total_branch) : 0);
     CK(cudaMemcpyAsync(h->h_out, h->d_out.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(&h->h_flag, static_cast<int32_t*>(h->d_counter.p) + 1, sizeof(int32_t),
+                       cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    if (h->h_flag != 0)
+        return fail(h, MCPHY_ERR_TIMEOUT, "a bounded wait in the fused kernel gave up (staging of step records)");
     if ((rc = finish_timing(h))) return rc;
     std::memcpy(ll, h->h_out, sizeof(double) * h->M);
     if (want_grad) std::memcpy(grad, h->h_out + h->M, sizeof(double) * h->total_branch);
@@ -537,8 +570,8 @@ int mcphy_destroy(mcphy_handle h) {
     if (!h) return MCPHY_ERR_ARG;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    DevBuf* bufs[] = {&h->d_desc, &h->d_sched, &h->d_items, &h->d_queue, &h->d_rows, &h->d_P,
-                      &h->d_dP, &h->d_codes, &h->d_dense, &h->d_params, &h->d_blen, &h->d_pgrad,
+    DevBuf* bufs[] = {&h->d_desc, &h->d_sched, &h->d_items, &h->d_queue, &h->d_steps,
+                      &h->d_recs, &h->d_codes, &h->d_dense, &h->d_params, &h->d_blen, &h->d_pgrad,
                       &h->d_pll, &h->d_part, &h->d_out, &h->d_post, &h->d_pre, &h->d_counter};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
@@ -782,6 +815,13 @@ int mcphy_set_stream(mcphy_handle h, void* stream) {
 int mcphy_synchronize(mcphy_handle h) {
     if (!h) return MCPHY_ERR_ARG;
     CK(cudaStreamSynchronize(h->stream));
+    if (h->d_counter.p) {
+        int32_t flag = 0;
+        CK(cudaMemcpy(&flag, static_cast<int32_t*>(h->d_counter.p) + 1, sizeof(int32_t),
+                      cudaMemcpyDeviceToHost));
+        if (flag != 0)
+            return fail(h, MCPHY_ERR_TIMEOUT, "a bounded wait in the fused kernel gave up (staging of step records)");
+    }
     return finish_timing(h);
 }
 

@@ -63,7 +63,8 @@ struct mcphy_engine {
     std::vector<int64_t> grad_offsets;   // M + 1
     int64_t total_branch = 0;
     int64_t n_items = 0;
-    int64_t n_prows = 0;
+    int64_t n_steps = 0;        // total schedule steps over all instances
+    int64_t rec_bytes_total = 0;
     int32_t max_J = 0;
     int32_t max_branch = 0;
     int64_t units = 0;
@@ -74,13 +75,14 @@ struct mcphy_engine {
     bool any_dense = false;
     std::vector<SchedNode> sched_all;
 
-    DevBuf d_desc, d_sched, d_items, d_queue, d_rows, d_P, d_dP, d_codes, d_dense, d_params,
+    DevBuf d_desc, d_sched, d_items, d_queue, d_steps, d_recs, d_codes, d_dense, d_params,
         d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter;
     int n_split = 1;
 
     double* h_blen = nullptr;
     size_t h_blen_cap = 0;
     double* h_out = nullptr;
+    int32_t h_flag = 0;
     size_t h_out_cap = 0;
 
     bool timing = false;

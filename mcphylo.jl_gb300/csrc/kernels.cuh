@@ -1,22 +1,28 @@
 // Device kernels of the likelihood / branch-gradient engine (sm_103a).
 //
-// Design (one evaluation = three launches):
-//   1. build_transition: P(t) and dP/dt for every (instance, branch, rate) from
-//      the FP64 eigensystem, in FP64, stored as Real
-//      (parallel_transition_prob / R_gemmturbo_large(_ptg)! / L_gemmturbo_large!,
-//      src/Likelihood/VectorizedFunctions.jl:89-168).
+// One evaluation = three launches:
+//   1. build_records: for every schedule step and rate category, a contiguous
+//      "step record": the step's operands and stack slots, and for each of its
+//      two child branches P(t)^T and dP/dt^T (FP64 arithmetic from the FP64
+//      eigensystem, stored as Real) plus a row of row sums (the Down vector of a
+//      leaf whose state is missing).  (parallel_transition_prob,
+//      R_gemmturbo_large(_ptg)!, L_gemmturbo_large!:
+//      src/Likelihood/VectorizedFunctions.jl:89-168.)
 //   2. prune: the fused post-order + pre-order sweep.  Sites are independent, so
-//      every warp owns a block of 32*SPT sites of one rate category of one
-//      instance and walks the WHOLE tree for them: no grid-wide barrier, no
-//      level-by-level launches.  Post-order partials go to a per-warp scratch
-//      column (written once, read back by the pre-order sweep); leaf data is
-//      read as compact state bitmasks.  The gradient terms of each branch are
-//      warp-reduced and written as one float per (work item, branch).
-//      (FelsensteinFunction, src/Likelihood/LikelihoodCalculator_Node.jl:3-114,
-//       comb_sum_product_loop!, by_max!, bymax!, root_sum, turbo_mul!,
-//       mygemmturbo!: VectorizedFunctions.jl:2-213)
-//   3. reduce: per (instance, branch) sum of the item partials in FP64, in a
-//      fixed order, so results are bit-reproducible run to run.
+//      every warp owns 32*SPT sites of one rate category of one instance and
+//      walks the WHOLE tree for them: no grid-wide barrier, no level launches.
+//      Step records stream into a per-warp double buffer in shared memory by TMA
+//      bulk copies (cp.async.bulk + mbarrier); post-order partials go to a
+//      per-warp global scratch column (written once, read back once by the
+//      pre-order sweep); stored pre-order partials use a small stack of slots;
+//      leaf children are a lookup of one row of P^T by the leaf's state code.
+//      The gradient terms of each branch are warp-reduced to one value per
+//      (work item, branch).  (FelsensteinFunction,
+//      src/Likelihood/LikelihoodCalculator_Node.jl:3-114; comb_sum_product_loop!,
+//      by_max!, bymax!, root_sum, turbo_mul!, mygemmturbo!:
+//      src/Likelihood/VectorizedFunctions.jl:2-213.)
+//   3. reduce: per (instance, branch) FP64 sums of the item partials in a fixed
+//      order (kernels_common.cu), so results are bit-reproducible run to run.
 //
 // Scaling: partials are rescaled by a power of two after every node (the
 // exponent of the per-site maximum) instead of by the maximum itself (by_max!).
@@ -31,16 +37,60 @@
 
 namespace mcphy {
 
+// ---------------------------------------------------------------- step records
+// Record of schedule step j for rate r (bytes):
+//   [0, 48)   int32 hdr[12] = {op0, op1, bpush, bpop, gr0, gr1, fpop, fpush,
+//                              pf0, pf1, 0, 0}
+//             gr_c: gradient index of child c's branch, -1 for a virtual branch;
+//             pf_c: operand c of step j - PF_DIST when it is internal, else -1
+//             (the pre-order sweep prefetches those post-order partials into L2)
+//   [48, ...) Real T[4][(KP+1)*KP]: T[2c] = P_c^T, T[2c+1] = dP_c^T for child c,
+//             rows 0..KP-1 are columns of the matrix, row KP holds the row sums
+//             over the K real states.
+constexpr int REC_HDR = 48;
+constexpr int PF_DIST = 6;
+__host__ __device__ constexpr int rec_mat(int kp) { return (kp + 1) * kp; }
+__host__ __device__ constexpr int rec_bytes(int kp, int real_bytes) {
+    return REC_HDR + 4 * rec_mat(kp) * real_bytes;
+}
+// steps per staged chunk: the largest power of two with <= 6 KB of records per buffer
+__host__ __device__ constexpr int chunk_steps(int kp, int real_bytes) {
+    return rec_bytes(kp, real_bytes) > 3072   ? 1
+           : rec_bytes(kp, real_bytes) > 1536 ? 2
+           : rec_bytes(kp, real_bytes) > 768  ? 4
+           : rec_bytes(kp, real_bytes) > 384  ? 8
+           : rec_bytes(kp, real_bytes) > 192  ? 16
+                                              : 32;
+}
+// Per-warp shared memory: two chunk buffers of step records, two chunk buffers of
+// leaf codes in schedule order (the leaf operands of the chunk's steps), a stack
+// of STACK_SMEM slots of partials (deeper slots live in global memory) and two
+// mbarriers.
+__host__ __device__ constexpr int vec_bytes(int kp, int spt, int real_bytes) {
+    return spt * 32 * kp * real_bytes;
+}
+__host__ __device__ constexpr int code_bytes(int kp) { return kp <= 8 ? 1 : 4; }
+// leaf codes of one step (two operands x the warp's 32*SPT sites)
+__host__ __device__ constexpr int tip_bytes(int kp, int spt) { return 2 * 32 * spt * code_bytes(kp); }
+__host__ __device__ constexpr int stack_smem_slots(int kp, int spt, int real_bytes) {
+    return vec_bytes(kp, spt, real_bytes) <= 1024 ? 6 : vec_bytes(kp, spt, real_bytes) <= 4096 ? 3 : 1;
+}
+// rounded to 128 bytes so every warp's TMA destinations stay aligned
+__host__ __device__ constexpr int warp_smem_bytes(int kp, int spt, int real_bytes) {
+    return (2 * chunk_steps(kp, real_bytes) * (rec_bytes(kp, real_bytes) + tip_bytes(kp, spt)) +
+            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 + 127) /
+           128 * 128;
+}
+
 struct PruneArgs {
     const InstanceDesc* inst;
-    const SchedNode* sched;
     const int2* items;        // (instance, local item index)
     const int32_t* queue;     // order in which warps take items
     int32_t n_items;
-    int32_t* counter;         // work counter, zeroed before the launch
-    const void* P;            // Real tables [row][rate][Kp][Kp], row-major in (s, s1)
-    const void* dP;
-    const void* codes;        // state bitmasks, type by Kp
+    int32_t* counter;         // [0] work counter, [1] error flag; zeroed before the launch
+    const unsigned char* recs;   // step records
+    const void* codes;        // state bitmasks in schedule order, type by Kp:
+                              // [block][step][operand][32*SPT] per instance
     const void* dense;        // Real [leaf_row][S_pad][Kp]
     const double* params;     // per-instance FP64 parameters
     void* post;               // Real scratch, [warp][node slot][SPT][32][Kp]
@@ -54,18 +104,17 @@ struct PruneArgs {
     int32_t want_grad;
 };
 
-struct BuildPArgs {
+struct BuildRecArgs {
     const InstanceDesc* inst;
-    const int2* rows;         // (instance, branch row) for every P row incl. identity
-    int32_t n_rows;
+    const SchedNode* sched;
+    const int2* steps;        // (instance, step j) for every step of every instance
+    int32_t n_steps;
     const double* params;
     const double* blen;
-    void* P;
-    void* dP;
+    unsigned char* recs;
     int32_t K;
     int32_t Kp;
     int32_t C;
-    int32_t want_grad;
 };
 
 struct ReduceArgs {
@@ -116,49 +165,39 @@ __device__ __forceinline__ double pow2_neg(double, int e) {
 
 template <typename Real> __device__ __forceinline__ Real rmax(Real a, Real b) { return a > b ? a : b; }
 
-// Rescale v by 2^-e (e = exponent of max v) and return e.  Exact.
+// Rescale v by 2^-e (e = unbiased exponent of max v, so the new maximum lies in
+// [1, 2)) and return the biased exponent field of the maximum (e + bias); the
+// caller subtracts the bias once per site.  Exact: a multiplication by a power
+// of two.  A zero maximum (an impossible site) leaves v at zero.
+__device__ __forceinline__ uint32_t scale_bits(float m, float& f) {
+    const uint32_t ex = __float_as_uint(m) & 0x7f800000u;
+    f = __uint_as_float(0x7f000000u - ex);                   // 2^(127 - field) = 2^-e
+    return ex >> 23;
+}
+__device__ __forceinline__ uint32_t scale_bits(double m, double& f) {
+    const unsigned long long ex = (unsigned long long)__double_as_longlong(m) & 0x7ff0000000000000ull;
+    f = __longlong_as_double((long long)(0x7fe0000000000000ull - ex));
+    return uint32_t(ex >> 52);
+}
+template <typename Real> struct ExpBias;
+template <> struct ExpBias<float> { static constexpr int value = 127; };
+template <> struct ExpBias<double> { static constexpr int value = 1023; };
+
 template <int KP, typename Real>
-__device__ __forceinline__ int rescale(Real (&v)[KP]) {
+__device__ __forceinline__ uint32_t rescale(Real (&v)[KP]) {
     Real m = v[0];
 #pragma unroll
     for (int k = 1; k < KP; ++k) m = rmax(m, v[k]);
-    int e = exponent_of(m);
-    Real f = pow2_neg(Real(0), e);
+    Real f;
+    const uint32_t field = scale_bits(m, f);
 #pragma unroll
     for (int k = 0; k < KP; ++k) v[k] *= f;
-    return e;
+    return field;
 }
 
-// Load / store KP Reals with the widest aligned vector access.
+// KP Reals from global or shared memory with the widest aligned vector access.
 template <int KP, typename Real>
-__device__ __forceinline__ void ld_vec(const Real* __restrict__ p, Real (&v)[KP]) {
-    if constexpr (sizeof(Real) == 4 && KP % 4 == 0) {
-#pragma unroll
-        for (int i = 0; i < KP / 4; ++i) {
-            float4 x = __ldg(reinterpret_cast<const float4*>(p) + i);
-            v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
-        }
-    } else if constexpr (sizeof(Real) == 4 && KP % 2 == 0) {
-#pragma unroll
-        for (int i = 0; i < KP / 2; ++i) {
-            float2 x = __ldg(reinterpret_cast<const float2*>(p) + i);
-            v[2 * i] = x.x; v[2 * i + 1] = x.y;
-        }
-    } else if constexpr (sizeof(Real) == 8 && KP % 2 == 0) {
-#pragma unroll
-        for (int i = 0; i < KP / 2; ++i) {
-            double2 x = __ldg(reinterpret_cast<const double2*>(p) + i);
-            v[2 * i] = x.x; v[2 * i + 1] = x.y;
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < KP; ++i) v[i] = __ldg(p + i);
-    }
-}
-
-// Scratch accesses are plain (coherent) loads: the same warp wrote them.
-template <int KP, typename Real>
-__device__ __forceinline__ void ld_scratch(const Real* p, Real (&v)[KP]) {
+__device__ __forceinline__ void ld_vec(const Real* p, Real (&v)[KP]) {
     if constexpr (sizeof(Real) == 4 && KP % 4 == 0) {
 #pragma unroll
         for (int i = 0; i < KP / 4; ++i) {
@@ -184,7 +223,33 @@ __device__ __forceinline__ void ld_scratch(const Real* p, Real (&v)[KP]) {
 }
 
 template <int KP, typename Real>
-__device__ __forceinline__ void st_scratch(Real* p, const Real (&v)[KP]) {
+__device__ __forceinline__ void ld_vec_nc(const Real* __restrict__ p, Real (&v)[KP]) {
+    if constexpr (sizeof(Real) == 4 && KP % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < KP / 4; ++i) {
+            float4 x = __ldg(reinterpret_cast<const float4*>(p) + i);
+            v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+        }
+    } else if constexpr (sizeof(Real) == 4 && KP % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < KP / 2; ++i) {
+            float2 x = __ldg(reinterpret_cast<const float2*>(p) + i);
+            v[2 * i] = x.x; v[2 * i + 1] = x.y;
+        }
+    } else if constexpr (sizeof(Real) == 8 && KP % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < KP / 2; ++i) {
+            double2 x = __ldg(reinterpret_cast<const double2*>(p) + i);
+            v[2 * i] = x.x; v[2 * i + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < KP; ++i) v[i] = __ldg(p + i);
+    }
+}
+
+template <int KP, typename Real>
+__device__ __forceinline__ void st_vec(Real* p, const Real (&v)[KP]) {
     if constexpr (sizeof(Real) == 4 && KP % 4 == 0) {
 #pragma unroll
         for (int i = 0; i < KP / 4; ++i)
@@ -203,80 +268,230 @@ __device__ __forceinline__ void st_scratch(Real* p, const Real (&v)[KP]) {
     }
 }
 
-// y[u] = M x[u] for SPT site vectors, M row-major KP x KP, rows streamed.
+// ---------------------------------------------------------------- mbarrier + TMA bulk
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// One elected lane: expect `bytes` and start the bulk copy global -> shared.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait for the phase with the given parity; false if it never completed.
+constexpr int kWaitLimit = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    for (int it = 0; it < kWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Staging: chunk x of CH steps (records, and for code-leaf instances the leaf
+// codes of those steps) lives in buffer x & 1; one mbarrier per buffer.
+template <int KP, typename Real, int SPT>
+struct Stage {
+    static constexpr int BYTES = rec_bytes(KP, sizeof(Real));
+    static constexpr int TIP = tip_bytes(KP, SPT);
+    static constexpr int CH = chunk_steps(KP, sizeof(Real));
+    unsigned char* base;        // record buffer 0, record buffer 1, tip buffer 0, tip buffer 1
+    uint64_t* bars;             // two mbarriers
+    uint32_t parity;            // bit b: phase parity expected next on buffer b
+    const unsigned char* src;   // records of the current (instance, rate)
+    const unsigned char* tsrc;  // leaf codes of the current (instance, site block), or null
+    int J;
+    int Q;                      // chunks
+    bool ok;
+
+    __device__ uint64_t* barrier(int b) const { return bars + b; }
+    __device__ void init(unsigned char* p, uint64_t* b, int lane) {
+        base = p;
+        bars = b;
+        parity = 0u;
+        ok = true;
+        if (lane == 0) {
+            mbar_init(barrier(0), 1);
+            mbar_init(barrier(1), 1);
+        }
+    }
+    // Lane 0 starts chunk x into its buffers; the warp must have finished reading
+    // them (__syncwarp before).
+    __device__ void issue(int x, int lane) {
+        if (lane == 0) {
+            const int first = x * CH;
+            const int n = min(CH, J - first);
+            const int b = x & 1;
+            const uint32_t rb = uint32_t(n * BYTES), tb = tsrc ? uint32_t(n * TIP) : 0u;
+            fence_proxy_async();
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         ::"r"(smem_u32(barrier(b))), "r"(rb + tb) : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                ::"r"(smem_u32(base + b * (CH * BYTES))), "l"(src + size_t(first) * BYTES), "r"(rb),
+                  "r"(smem_u32(barrier(b))) : "memory");
+            if (tb)
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                    ::"r"(smem_u32(base + 2 * CH * BYTES + b * (CH * TIP))),
+                      "l"(tsrc + size_t(first) * TIP), "r"(tb), "r"(smem_u32(barrier(b))) : "memory");
+        }
+    }
+    // Waits for chunk x (the next phase of its buffer).  Warp-uniform result.
+    __device__ bool wait(int x) {
+        const int b = x & 1;
+        bool done = mbar_wait(barrier(b), (parity >> b) & 1u);
+        done = __all_sync(0xffffffffu, done);
+        if (done) parity ^= (1u << b);
+        ok = ok && done;
+        return done;
+    }
+    __device__ const unsigned char* rec(int j) const {
+        return base + ((j / CH) & 1) * (CH * BYTES) + (j % CH) * BYTES;
+    }
+    // leaf codes of operand c of step j
+    __device__ const unsigned char* tip(int j, int c) const {
+        return base + 2 * CH * BYTES + ((j / CH) & 1) * (CH * TIP) + (j % CH) * TIP +
+               c * (TIP / 2);
+    }
+};
+
+__device__ __forceinline__ void rec_header(const unsigned char* r, int (&h)[8]) {
+    const int4 a = reinterpret_cast<const int4*>(r)[0];
+    const int4 b = reinterpret_cast<const int4*>(r)[1];
+    h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+    h[4] = b.x; h[5] = b.y; h[6] = b.z; h[7] = b.w;
+}
+__device__ __forceinline__ int2 rec_prefetch(const unsigned char* r) {
+    return reinterpret_cast<const int2*>(r)[4];
+}
+template <int KP, typename Real>
+__device__ __forceinline__ const Real* rec_mat_ptr(const unsigned char* r, int which) {
+    return reinterpret_cast<const Real*>(r + REC_HDR) + which * rec_mat(KP);
+}
+// Bulk prefetch of a contiguous range into L2 (one lane).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// D[u] = M L[u] with M given transposed (rows of T are columns of M).
 template <int KP, int SPT, typename Real>
-__device__ __forceinline__ void matvec(const Real* __restrict__ M, const Real (&x)[SPT][KP],
-                                       Real (&y)[SPT][KP]) {
+__device__ __forceinline__ void apply_t(const Real* T, const Real (&L)[SPT][KP], Real (&D)[SPT][KP]) {
 #pragma unroll
-    for (int s = 0; s < KP; ++s) {
+    for (int u = 0; u < SPT; ++u)
+#pragma unroll
+        for (int s = 0; s < KP; ++s) D[u][s] = Real(0);
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
         Real row[KP];
-        ld_vec<KP>(M + s * KP, row);
+        ld_vec<KP>(T + k * KP, row);
+#pragma unroll
+        for (int u = 0; u < SPT; ++u)
+#pragma unroll
+            for (int s = 0; s < KP; ++s) D[u][s] = fma(row[s], L[u][k], D[u][s]);
+    }
+}
+
+// y[u] = M^T x[u] with M given transposed: y[k] = row_k(T) . x.
+template <int KP, int SPT, typename Real>
+__device__ __forceinline__ void apply_tt(const Real* T, const Real (&x)[SPT][KP], Real (&y)[SPT][KP]) {
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+        Real row[KP];
+        ld_vec<KP>(T + k * KP, row);
 #pragma unroll
         for (int u = 0; u < SPT; ++u) {
             Real acc = Real(0);
 #pragma unroll
-            for (int k = 0; k < KP; ++k) acc = fma(row[k], x[u][k], acc);
-            y[u][s] = acc;
+            for (int s = 0; s < KP; ++s) acc = fma(row[s], x[u][s], acc);
+            y[u][k] = acc;
         }
     }
 }
 
-// y[u] = M^T x[u] (the pre-order step P^T * pre, mygemmturbo! with transpose).
-template <int KP, int SPT, typename Real>
-__device__ __forceinline__ void matvec_t(const Real* __restrict__ M, const Real (&x)[SPT][KP],
-                                         Real (&y)[SPT][KP]) {
+// A leaf operand is kept as the row of P^T it selects (0..K-1: one state; KP:
+// every state, the row sums) when the instance has no partially ambiguous codes,
+// else as the raw state bitmask; either way in the bits of L[u][0], so that an
+// operand costs SPT*KP registers whatever its kind.
+__device__ __forceinline__ float u32_bits(uint32_t c, float) { return __uint_as_float(c); }
+__device__ __forceinline__ double u32_bits(uint32_t c, double) { return __longlong_as_double((long long)c); }
+__device__ __forceinline__ uint32_t bits_u32(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ uint32_t bits_u32(double v) { return uint32_t(__double_as_longlong(v)); }
+
+template <int KP>
+__device__ __forceinline__ uint32_t leaf_row(uint32_t code, uint32_t allmask) {
+    return code == allmask ? uint32_t(KP) : uint32_t(__ffs(int(code)) - 1);
+}
+
+// Sum of the rows of T selected by a state bitmask (a partially ambiguous leaf).
+template <int KP, typename Real>
+__device__ __forceinline__ void leaf_down_mask(const Real* T, uint32_t code, Real (&D)[KP]) {
 #pragma unroll
-    for (int u = 0; u < SPT; ++u)
+    for (int s = 0; s < KP; ++s) D[s] = Real(0);
+    for (int k = 0; k < KP; ++k) {
+        if ((code >> k) & 1u) {
+            Real row[KP];
+            ld_vec<KP>(T + k * KP, row);
 #pragma unroll
-        for (int k = 0; k < KP; ++k) y[u][k] = Real(0);
-#pragma unroll
-    for (int s = 0; s < KP; ++s) {
-        Real row[KP];
-        ld_vec<KP>(M + s * KP, row);
-#pragma unroll
-        for (int u = 0; u < SPT; ++u)
-#pragma unroll
-            for (int k = 0; k < KP; ++k) y[u][k] = fma(row[k], x[u][s], y[u][k]);
+            for (int s = 0; s < KP; ++s) D[s] += row[s];
+        }
     }
 }
 
-// Operand of a schedule node for SPT sites: a leaf (bitmask or dense) or an
-// internal post-order partial from the warp's scratch column.
+// A warp vector (post-order slot, dense leaf block or stack slot) in shared or
+// global memory: the lane's partial for site u is at (u*32 + lane)*KP.
 template <int KP, int SPT, typename Real>
-__device__ __forceinline__ void load_operand(int op, const InstanceDesc& d, const void* codes,
-                                             const void* dense, const Real* post, int site0,
-                                             int lane, Real (&L)[SPT][KP]) {
-    if (op < 0) {
-        const int64_t row = int64_t(-op - 1);
-        if (d.dense) {
-            const Real* base = reinterpret_cast<const Real*>(dense) + d.leaf_off;
+__device__ __forceinline__ void read_vec(const Real* v, int lane, Real (&L)[SPT][KP]) {
 #pragma unroll
-            for (int u = 0; u < SPT; ++u)
-                ld_vec<KP>(base + (row * d.S_pad + site0 + 32 * u) * KP, L[u]);
-        } else {
-            using Code = typename CodeOf<KP>::type;
-            const Code* base = reinterpret_cast<const Code*>(codes) + d.leaf_off + row * d.S_pad;
+    for (int u = 0; u < SPT; ++u) ld_vec<KP>(v + (u * 32 + lane) * KP, L[u]);
+}
+template <int KP, int SPT, typename Real>
+__device__ __forceinline__ void write_vec(Real* v, int lane, const Real (&L)[SPT][KP]) {
 #pragma unroll
-            for (int u = 0; u < SPT; ++u) {
-                uint32_t c = uint32_t(__ldg(base + site0 + 32 * u));
+    for (int u = 0; u < SPT; ++u) st_vec<KP>(v + (u * 32 + lane) * KP, L[u]);
+}
+// Leaf codes of the warp's sites in a ring slot -> row indices (or bitmasks).
+template <int KP, int SPT, typename Real>
+__device__ __forceinline__ void read_codes(const unsigned char* p, int lane, bool ambig,
+                                           uint32_t allmask, Real (&L)[SPT][KP]) {
+    using Code = typename CodeOf<KP>::type;
 #pragma unroll
-                for (int k = 0; k < KP; ++k) L[u][k] = ((c >> k) & 1u) ? Real(1) : Real(0);
-            }
-        }
+    for (int u = 0; u < SPT; ++u) {
+        const uint32_t c = uint32_t(reinterpret_cast<const Code*>(p)[u * 32 + lane]);
+        L[u][0] = u32_bits(ambig ? c : leaf_row<KP>(c, allmask), Real(0));
+    }
+}
+
+// Down vectors (or dD = dP L) of an operand through one table T of a child.
+template <int KP, int SPT, typename Real>
+__device__ __forceinline__ void down(const Real (&L)[SPT][KP], bool code_leaf, bool ambig,
+                                     const Real* T, Real (&D)[SPT][KP]) {
+    if (!code_leaf) {
+        apply_t<KP, SPT>(T, L, D);
+    } else if (!ambig) {
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) ld_vec<KP>(T + bits_u32(L[u][0]) * KP, D[u]);
     } else {
-        const Real* p = post + (int64_t(op) * SPT * 32 + lane) * KP;
 #pragma unroll
-        for (int u = 0; u < SPT; ++u) ld_scratch<KP>(p + u * 32 * KP, L[u]);
+        for (int u = 0; u < SPT; ++u) leaf_down_mask<KP>(T, bits_u32(L[u][0]), D[u]);
     }
-}
-
-__device__ __forceinline__ SchedNode load_sched(const SchedNode* p) {
-    const int4* q = reinterpret_cast<const int4*>(p);
-    int4 a = __ldg(q), b = __ldg(q + 1);
-    SchedNode n;
-    n.op[0] = a.x; n.op[1] = a.y; n.br[0] = a.z; n.br[1] = a.w;
-    n.ps[0] = b.x; n.ps[1] = b.y; n.self_slot = b.z; n.pad = b.w;
-    return n;
 }
 
 // d log L_site / dt = num / den.  FP32: fast reciprocal-multiply (2 ulp), well
@@ -287,7 +502,6 @@ __device__ __forceinline__ double ratio(double n, double d) { return n / d; }
 __device__ __forceinline__ float log_real(float x) { return logf(x); }
 __device__ __forceinline__ double log_real(double x) { return log(x); }
 
-// ---------------------------------------------------------------- fused sweep
 template <int SPT, int KP, typename Real>
 __device__ __forceinline__ void copy_part(Real (&dst)[SPT][KP], const Real (&src)[SPT][KP]) {
 #pragma unroll
@@ -296,21 +510,45 @@ __device__ __forceinline__ void copy_part(Real (&dst)[SPT][KP], const Real (&src
         for (int k = 0; k < KP; ++k) dst[u][k] = src[u][k];
 }
 
-// One warp = 32*SPT sites of one rate category of one instance.  Both sweeps
-// are software-pipelined: the schedule entry and the operands of the next step
-// are loaded before the current step computes, and a partial produced by one
-// step and consumed by the next (the right child in post-order; the next node's
-// pre-order partial in the backward sweep) stays in registers.
+// ---------------------------------------------------------------- fused sweep
+// One warp = 32*SPT sites of one rate category of one instance.  Step records and
+// the leaf codes of the steps arrive in chunks of CH steps by TMA bulk copies
+// into a double buffer in shared memory (one wait and one refill per chunk).
+// Post-order sweep: operand 1 of a step is a leaf or the previous step's partial
+// (kept in registers), operand 0 a leaf or a partial popped from the stack; the
+// partials are also written to the warp's global column for the pre-order sweep.
+// Pre-order sweep: internal operands are read back from that column one step
+// ahead; the pre-order partial of operand 1 (the next step) stays in registers
+// and that of operand 0 goes on the stack.
 template <int KP, typename Real, int SPT>
 __global__ void __launch_bounds__(256)
 prune_kernel(const PruneArgs a) {
+    using St = Stage<KP, Real, SPT>;
+    constexpr int CH = St::CH;
+    constexpr int NS = stack_smem_slots(KP, SPT, sizeof(Real));
+    constexpr int SLOT = SPT * 32 * KP;             // Real elements per warp vector
+    extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31;
-    const int64_t gw = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int wib = threadIdx.x >> 5;
+    const int64_t gw = int64_t(blockIdx.x) * (blockDim.x >> 5) + wib;
     Real* post = reinterpret_cast<Real*>(a.post) + gw * a.warp_stride;
-    Real* pre = reinterpret_cast<Real*>(a.pre) + gw * a.pre_warp_stride;
+    Real* gstack = reinterpret_cast<Real*>(a.pre) + gw * a.pre_warp_stride;
     const int C = a.C;
-    const int64_t slot = int64_t(SPT) * 32 * KP;   // Real elements per schedule slot
+    const uint32_t allmask = (a.K >= 32) ? 0xffffffffu : ((1u << a.K) - 1u);
     constexpr double LN2 = 0.6931471805599453094;
+
+    unsigned char* wbase = smem + size_t(wib) * warp_smem_bytes(KP, SPT, int(sizeof(Real)));
+    Real* sstack = reinterpret_cast<Real*>(wbase + 2 * CH * (St::BYTES + St::TIP));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
+                                                  NS * SLOT * sizeof(Real));
+    St st;
+    st.init(wbase, bars, lane);
+    if (lane == 0) fence_mbar_init();
+    __syncwarp();
+    // stack slot s: shared memory below NS, the warp's global column above
+    auto stack_ptr = [&](int s) -> Real* {
+        return s < NS ? sstack + s * SLOT : gstack + int64_t(s) * SLOT;
+    };
 
     for (;;) {
         int t = 0;
@@ -323,97 +561,141 @@ prune_kernel(const PruneArgs a) {
         const int r = it.y / d.n_blocks;
         const int blk = it.y - r * d.n_blocks;
         const int site0 = blk * (32 * SPT) + lane;
-        const SchedNode* sch = a.sched + d.sched_off;
-        const int64_t pstride = int64_t(C) * KP * KP;
-        const Real* Pt = reinterpret_cast<const Real*>(a.P) + d.p_off + int64_t(r) * KP * KP;
-        const Real* dPt = reinterpret_cast<const Real*>(a.dP) + d.p_off + int64_t(r) * KP * KP;
         const double* pi_d = a.params + d.param_off + 2 * a.K * a.K + a.K + 1 + C;
         const int J = d.J;
+        const bool code_leaves = !d.dense;
+        const bool ambig = d.ambig != 0;
+        const Real* dense = reinterpret_cast<const Real*>(a.dense) + d.leaf_off;
 
         bool valid[SPT];
 #pragma unroll
         for (int u = 0; u < SPT; ++u) valid[u] = (site0 + 32 * u) < d.S;
 
-        // ---------------- post-order sweep (logL)
-        int eacc[SPT];
+        // operand c of step j when it is a leaf, into L
+        auto leaf = [&](int j, int c, int op, Real (&L)[SPT][KP]) {
+            if (code_leaves) {
+                read_codes<KP, SPT>(st.tip(j, c), lane, ambig, allmask, L);
+            } else {
+                const int64_t row = int64_t(-op - 1);
 #pragma unroll
-        for (int u = 0; u < SPT; ++u) eacc[u] = 0;
-        double ll_lane = 0.0;
-        SchedNode nd = load_sched(sch);
-        Real La[SPT][KP], Lb[SPT][KP];
-        load_operand<KP, SPT>(nd.op[0], d, a.codes, a.dense, post, site0, lane, La);
-        load_operand<KP, SPT>(nd.op[1], d, a.codes, a.dense, post, site0, lane, Lb);
-        for (int j = 0; j < J; ++j) {
-            const bool has_next = j + 1 < J;
-            SchedNode nn = nd;
-            Real Na[SPT][KP], Nb[SPT][KP];
-            if (has_next) {
-                nn = load_sched(sch + j + 1);
-                if (nn.op[0] != j) load_operand<KP, SPT>(nn.op[0], d, a.codes, a.dense, post, site0, lane, Na);
-                if (nn.op[1] != j) load_operand<KP, SPT>(nn.op[1], d, a.codes, a.dense, post, site0, lane, Nb);
+                for (int u = 0; u < SPT; ++u)
+                    ld_vec_nc<KP>(dense + (row * d.S_pad + site0 + 32 * u) * KP, L[u]);
             }
+        };
+
+        st.src = a.recs + d.rec_off + size_t(r) * size_t(J) * St::BYTES;
+        st.tsrc = code_leaves ? reinterpret_cast<const unsigned char*>(a.codes) + d.leaf_off +
+                                    size_t(blk) * size_t(J) * St::TIP
+                              : nullptr;
+        st.J = J;
+        st.Q = (J + CH - 1) / CH;
+        __syncwarp();
+        st.issue(0, lane);
+        if (st.Q > 1) st.issue(1, lane);
+
+        // ---------------- post-order sweep (logL)
+        uint32_t eacc[SPT];
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) eacc[u] = 0u;
+        double ll_lane = 0.0;
+        Real Lp[SPT][KP];          // the previous step's partial
+        for (int j = 0; j < J; ++j) {
+            if (j % CH == 0 && !st.wait(j / CH)) break;
+            const unsigned char* rj = st.rec(j);
+            int h[8];
+            rec_header(rj, h);
+            Real A[SPT][KP], B[SPT][KP];
+            if (h[0] >= 0) read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
+            else leaf(j, 0, h[0], A);
+            if (h[1] >= 0) copy_part(B, Lp);
+            else leaf(j, 1, h[1], B);
             Real Da[SPT][KP], Db[SPT][KP];
-            matvec<KP, SPT>(Pt + nd.br[0] * pstride, La, Da);
-            matvec<KP, SPT>(Pt + nd.br[1] * pstride, Lb, Db);
+            down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), Da);
+            down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), Db);
 #pragma unroll
             for (int u = 0; u < SPT; ++u) {
 #pragma unroll
                 for (int k = 0; k < KP; ++k) Da[u][k] *= Db[u][k];
                 eacc[u] += rescale<KP>(Da[u]);
             }
-            if (has_next) {
-                Real* p = post + int64_t(j) * slot + lane * KP;
-#pragma unroll
-                for (int u = 0; u < SPT; ++u) st_scratch<KP>(p + u * 32 * KP, Da[u]);
-                if (nn.op[0] == j) copy_part(La, Da); else copy_part(La, Na);
-                if (nn.op[1] == j) copy_part(Lb, Da); else copy_part(Lb, Nb);
-                nd = nn;
+            if (j + 1 < J) {
+                // the post-order column is only read back by the gradient sweep
+                if (a.want_grad) write_vec<KP, SPT>(post + int64_t(j) * SLOT, lane, Da);
+                if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Da);
+                copy_part(Lp, Da);
             } else {
 #pragma unroll
                 for (int u = 0; u < SPT; ++u) {
                     Real lik = Real(0);
 #pragma unroll
                     for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Da[u][k], lik);
-                    double v = double(log_real(lik)) + double(eacc[u]) * LN2;
+                    const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
+                    const double v = double(log_real(lik)) + double(ex) * LN2;
                     ll_lane += valid[u] ? v : 0.0;
                 }
             }
+            // chunk finished: refill its buffers with the chunk after next
+            if ((j + 1) % CH == 0 || j + 1 == J) {
+                __syncwarp();
+                if (j / CH + 2 < st.Q) st.issue(j / CH + 2, lane);
+            }
         }
+        if (!st.ok) break;
         ll_lane = warp_sum(ll_lane);
         if (lane == 0) a.pll[item] = ll_lane;
-        if (!a.want_grad) continue;
+        if (!a.want_grad) continue;   // every issued chunk has been waited for
 
         // ---------------- pre-order sweep (gradient)
+        // buffers hold chunks Q-1 and Q-2 (both waited for)
         Real* pg = reinterpret_cast<Real*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
-        nd = load_sched(sch + (J - 1));
-        Real pb[SPT][KP];
+        int low = st.Q >= 2 ? st.Q - 2 : 0;   // lowest chunk waited for
+        int h[8];
+        rec_header(st.rec(J - 1), h);
+        Real pb[SPT][KP], NA[SPT][KP], NB[SPT][KP];
 #pragma unroll
         for (int u = 0; u < SPT; ++u)
 #pragma unroll
             for (int k = 0; k < KP; ++k) pb[u][k] = Real(__ldg(pi_d + k));
-        load_operand<KP, SPT>(nd.op[0], d, a.codes, a.dense, post, site0, lane, La);
-        load_operand<KP, SPT>(nd.op[1], d, a.codes, a.dense, post, site0, lane, Lb);
+        if (lane == 0) {
+            // the first PF_DIST steps' post-order partials (later ones: from the records)
+            for (int q = 0; q < PF_DIST && q < CH && q < J; ++q) {
+                int hq[8];
+                rec_header(st.rec(J - 1 - q), hq);
+                for (int c = 0; c < 2; ++c)
+                    if (hq[c] >= 0) prefetch_l2(post + int64_t(hq[c]) * SLOT, SLOT * sizeof(Real));
+            }
+        }
+        if (h[0] >= 0) read_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, NA);
+        if (h[1] >= 0) read_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, NB);
         for (int j = J - 1; j >= 0; --j) {
-            const bool has_next = j > 0;
-            SchedNode nn = nd;
-            Real Na[SPT][KP], Nb[SPT][KP], Npb[SPT][KP];
-            // the next node (j-1) is a child of this one -> its pre-order partial
-            // is produced below and carried in registers; else it was stored
-            // when its parent (processed earlier) ran
-            const bool carry = has_next && (nd.op[0] == j - 1 || nd.op[1] == j - 1);
-            if (has_next) {
-                nn = load_sched(sch + (j - 1));
-                load_operand<KP, SPT>(nn.op[0], d, a.codes, a.dense, post, site0, lane, Na);
-                load_operand<KP, SPT>(nn.op[1], d, a.codes, a.dense, post, site0, lane, Nb);
-                if (!carry) {
-                    const Real* p = pre + int64_t(nn.self_slot) * slot + lane * KP;
-#pragma unroll
-                    for (int u = 0; u < SPT; ++u) ld_scratch<KP>(p + u * 32 * KP, Npb[u]);
+            const unsigned char* rj = st.rec(j);
+            if (lane == 0) {
+                const int2 pf = rec_prefetch(rj);
+                if (pf.x >= 0) prefetch_l2(post + int64_t(pf.x) * SLOT, SLOT * sizeof(Real));
+                if (pf.y >= 0) prefetch_l2(post + int64_t(pf.y) * SLOT, SLOT * sizeof(Real));
+            }
+            Real A[SPT][KP], B[SPT][KP];
+            if (h[0] >= 0) copy_part(A, NA);
+            else leaf(j, 0, h[0], A);
+            if (h[1] >= 0) copy_part(B, NB);
+            else leaf(j, 1, h[1], B);
+            if (h[3] >= 0) read_vec<KP, SPT>(stack_ptr(h[3]), lane, pb);   // else carried
+            // operands of the next step, one step ahead
+            int hn[8];
+            if (j > 0) {
+                const int qn = (j - 1) / CH;
+                if (qn < low) {
+                    if (!st.wait(qn)) break;
+                    low = qn;
                 }
+                rec_header(st.rec(j - 1), hn);
+                if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, NA);
+                if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, NB);
             }
             Real D[2][SPT][KP];
-            matvec<KP, SPT>(Pt + nd.br[0] * pstride, La, D[0]);
-            matvec<KP, SPT>(Pt + nd.br[1] * pstride, Lb, D[1]);
+            down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), D[0]);
+            down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
+            Real Npb[SPT][KP];
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 // pre-order partial at the top of branch c: mother's pre times the
@@ -423,10 +705,10 @@ prune_kernel(const PruneArgs a) {
                 for (int u = 0; u < SPT; ++u)
 #pragma unroll
                     for (int k = 0; k < KP; ++k) pt[u][k] = pb[u][k] * D[1 - c][u][k];
-                if (nd.br[c] < d.n_branch) {   // real branch: gradient entry br[c]
+                if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
-                    if (c == 0) matvec<KP, SPT>(dPt + nd.br[0] * pstride, La, dD);
-                    else matvec<KP, SPT>(dPt + nd.br[1] * pstride, Lb, dD);
+                    if (c == 0) down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
+                    else down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 3), dD);
                     Real g = Real(0);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
@@ -439,78 +721,121 @@ prune_kernel(const PruneArgs a) {
                         g += valid[u] ? ratio(num, den) : Real(0);
                     }
                     g = warp_sum(g);
-                    if (lane == 0) pg[nd.br[c]] = g;
+                    if (lane == 0) pg[h[4 + c]] = g;
                 }
-                if (nd.op[c] >= 0) {
+                if (h[c] >= 0) {
                     Real pbc[SPT][KP];
-                    matvec_t<KP, SPT>(Pt + nd.br[c] * pstride, pt, pbc);
+                    apply_tt<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 2 * c), pt, pbc);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) rescale<KP>(pbc[u]);
-                    if (nd.ps[c] < 0) {
-                        copy_part(Npb, pbc);      // child c is step j-1
-                    } else {
-                        Real* p = pre + int64_t(nd.ps[c]) * slot + lane * KP;
-#pragma unroll
-                        for (int u = 0; u < SPT; ++u) st_scratch<KP>(p + u * 32 * KP, pbc[u]);
-                    }
+                    if (c == 1) copy_part(Npb, pbc);                             // step j-1
+                    else write_vec<KP, SPT>(stack_ptr(h[2]), lane, pbc);
                 }
             }
-            if (has_next) {
-                nd = nn;
-                copy_part(La, Na);
-                copy_part(Lb, Nb);
-                copy_part(pb, Npb);
+            if (h[1] >= 0) copy_part(pb, Npb);
+            // chunk finished (descending): refill its buffers two chunks below
+            if (j % CH == 0) {
+                __syncwarp();
+                if (j / CH - 2 >= 0) st.issue(j / CH - 2, lane);
+            }
+            if (j > 0) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) h[q] = hn[q];
             }
         }
+        if (!st.ok) break;
+    }
+    if (!st.ok) {
+        // a bounded wait gave up: report, and let the copies this warp issued land
+        // (bounded as well) before its shared memory is released
+        if (lane == 0) atomicExch(a.counter + 1, 1);
+        mbar_wait(st.barrier(0), st.parity & 1u);
+        mbar_wait(st.barrier(1), (st.parity >> 1) & 1u);
     }
 }
 
-// ---------------------------------------------------------------- P(t), dP/dt
-// One thread per (P row, rate, state s).  FP64 arithmetic in the reference's
-// order: out2[m,i] = U[m,i] * exp(mu * t * D[i] * rate); P = out2 * Uinv.
+// ---------------------------------------------------------------- step records
+// One thread per (step record, child, rate): P(t) and dP/dt of the child's branch
+// in FP64, in the reference's order (out2[m,i] = U[m,i] * exp(mu * t * D[i] * rate);
+// P = out2 * Uinv), written transposed with the row-sum row; identity for the
+// zero-length virtual branches.  The c == 0 thread also writes the header.
 template <typename Real>
-__global__ void build_transition_kernel(const BuildPArgs a) {
+__global__ void build_records_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, Kp = a.Kp, C = a.C;
-    const int64_t total = int64_t(a.n_rows) * C * Kp;
-    if (tid >= total) return;
-    const int s = int(tid % Kp);
-    const int r = int((tid / Kp) % C);
-    const int row = int(tid / (int64_t(Kp) * C));
-    const int2 ib = a.rows[row];
-    const InstanceDesc& d = a.inst[ib.x];
-    const int b = ib.y;
-    Real* P = reinterpret_cast<Real*>(a.P) + d.p_off + ((int64_t(b) * C + r) * Kp + s) * Kp;
-    Real* dP = reinterpret_cast<Real*>(a.dP) + d.p_off + ((int64_t(b) * C + r) * Kp + s) * Kp;
-    if (b >= d.n_branch || s >= K) {
-        for (int s1 = 0; s1 < Kp; ++s1) {
-            P[s1] = Real(s1 == s ? 1 : 0);
-            if (a.want_grad) dP[s1] = Real(0);
+    if (tid >= int64_t(a.n_steps) * 2 * C) return;
+    const int r = int(tid % C);
+    const int c = int((tid / C) % 2);
+    const int2 sj = a.steps[tid / (2 * C)];
+    const InstanceDesc& d = a.inst[sj.x];
+    const int j = sj.y;
+    const SchedNode sn = a.sched[d.sched_off + j];
+    const int bytes = rec_bytes(Kp, sizeof(Real));
+    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(bytes);
+    if (c == 0) {
+        int* hd = reinterpret_cast<int*>(rec);
+        hd[0] = sn.op[0];
+        hd[1] = sn.op[1];
+        hd[2] = sn.bpush;
+        hd[3] = sn.bpop;
+        hd[4] = sn.br[0] < d.n_branch ? sn.br[0] : -1;
+        hd[5] = sn.br[1] < d.n_branch ? sn.br[1] : -1;
+        hd[6] = sn.fpop;
+        hd[7] = sn.fpush;
+        // internal operands of the step PF_DIST later in the pre-order sweep
+        const int jp = j - PF_DIST;
+        const SchedNode snp = a.sched[d.sched_off + (jp >= 0 ? jp : 0)];
+        hd[8] = (jp >= 0 && snp.op[0] >= 0) ? snp.op[0] : -1;
+        hd[9] = (jp >= 0 && snp.op[1] >= 0) ? snp.op[1] : -1;
+        hd[10] = 0;
+        hd[11] = 0;
+    }
+    const int mat = rec_mat(Kp);
+    Real* PT = reinterpret_cast<Real*>(rec + REC_HDR) + (2 * c) * mat;
+    Real* dPT = PT + mat;
+    const int b = sn.br[c];
+    if (b >= d.n_branch) {
+        for (int s = 0; s < Kp; ++s) {
+            for (int k = 0; k < Kp; ++k) {
+                PT[k * Kp + s] = Real(k == s ? 1 : 0);
+                dPT[k * Kp + s] = Real(0);
+            }
+            PT[Kp * Kp + s] = Real(s < K ? 1 : 0);
+            dPT[Kp * Kp + s] = Real(0);
         }
         return;
     }
     const double* U = a.params + d.param_off;
-    const double* D = U + K * K;
-    const double* Uinv = D + K;
+    const double* Dv = U + K * K;
+    const double* Uinv = Dv + K;
     const double mu = Uinv[K * K];
     const double rate = Uinv[K * K + 1 + r];
     const double t = a.blen[d.blen_off + b];
     double e[32], de[32];
-    for (int k = 0; k < K; ++k) {
-        double x = exp(mu * t * D[k] * rate);
-        e[k] = U[s + K * k] * x;
-        de[k] = U[s + K * k] * D[k] * rate * mu * x;
+    for (int m = 0; m < K; ++m) {
+        const double x = exp(mu * t * Dv[m] * rate);
+        e[m] = x;
+        de[m] = Dv[m] * rate * mu * x;
     }
-    for (int s1 = 0; s1 < Kp; ++s1) {
-        double p = 0.0, dp = 0.0;
-        if (s1 < K) {
-            for (int k = 0; k < K; ++k) {
-                p += e[k] * Uinv[k + K * s1];
-                dp += de[k] * Uinv[k + K * s1];
+    for (int s = 0; s < Kp; ++s) {
+        double rs = 0.0, drs = 0.0;
+        for (int k = 0; k < Kp; ++k) {
+            double p = 0.0, dp = 0.0;
+            if (s < K && k < K) {
+                for (int m = 0; m < K; ++m) {
+                    p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                    dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+                }
+                rs += p;
+                drs += dp;
+            } else {
+                p = (s == k) ? 1.0 : 0.0;
             }
+            PT[k * Kp + s] = Real(p);
+            dPT[k * Kp + s] = Real(dp);
         }
-        P[s1] = Real(p);
-        if (a.want_grad) dP[s1] = Real(dp);
+        PT[Kp * Kp + s] = Real(rs);
+        dPT[Kp * Kp + s] = Real(drs);
     }
 }
 
@@ -526,7 +851,7 @@ cudaError_t launch_prune_f64(int Kp, int spt, int blocks, int tpb, const PruneAr
                              cudaStream_t st);
 cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, int* blocks_per_sm);
 cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, int* blocks_per_sm);
-cudaError_t launch_build_p(bool f64, const BuildPArgs& a, cudaStream_t st);
+cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st);
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st);
 
 }  // namespace mcphy

@@ -76,15 +76,15 @@ cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_p(bool f64, const BuildPArgs& a, cudaStream_t st) {
-    const int64_t total = int64_t(a.n_rows) * a.C * a.Kp;
+cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st) {
+    const int64_t total = int64_t(a.n_steps) * 2 * a.C;
     if (total == 0) return cudaSuccess;
     const int tpb = 128;
     const int64_t blocks = (total + tpb - 1) / tpb;
     if (f64)
-        build_transition_kernel<double><<<unsigned(blocks), tpb, 0, st>>>(a);
+        build_records_kernel<double><<<unsigned(blocks), tpb, 0, st>>>(a);
     else
-        build_transition_kernel<float><<<unsigned(blocks), tpb, 0, st>>>(a);
+        build_records_kernel<float><<<unsigned(blocks), tpb, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -5,7 +5,11 @@ namespace mcphy {
 
 template <int KP, int SPT>
 static cudaError_t go(int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
-    prune_kernel<KP, double, SPT><<<blocks, tpb, 0, st>>>(a);
+    const int smem = (tpb / 32) * warp_smem_bytes(KP, SPT, int(sizeof(double)));
+    cudaError_t e = cudaFuncSetAttribute(prune_kernel<KP, double, SPT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    prune_kernel<KP, double, SPT><<<blocks, tpb, smem, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -38,7 +42,10 @@ cudaError_t launch_prune_f64(int Kp, int spt, int blocks, int tpb, const PruneAr
 cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, int* bps) {
     const void* f = pick(Kp, spt);
     if (!f) return cudaErrorInvalidValue;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, f, tpb, 0);
+    const int smem = (tpb / 32) * warp_smem_bytes(Kp, spt, int(sizeof(double)));
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, f, tpb, smem);
 }
 
 }  // namespace mcphy

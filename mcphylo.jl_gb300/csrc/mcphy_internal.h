@@ -10,25 +10,30 @@
 namespace mcphy {
 
 // One binary internal node of the kernel schedule, in post-order (a proper DFS
-// post-order of the binarised tree).  Schedule index j is also the node's slot in
-// the per-warp post-order scratch; the root is j = J-1.
-//   op[c] >= 0 : child c is internal schedule node op[c]
+// post-order of the binarised tree, heavier subtree first).  Schedule index j is
+// also the node's slot in the per-warp post-order scratch; the root is j = J-1.
+//   op[c] >= 0 : child c is internal schedule node op[c]; op[1] >= 0 implies
+//                op[1] == j-1 (the builder puts the previous step in position 1)
 //   op[c] <  0 : child c is leaf row (-op[c]-1) of the instance's leaf table
-//   br[c]      : row of the instance's P/dP table for the branch above child c,
-//                equal to the gradient index node.num - 1; the last row (index
-//                n_branch) is the identity used for the zero-length "virtual"
-//                branches that binarise multifurcations (no gradient output)
-//   ps[c]      : pre-order stack slot where the backward sweep leaves child c's
-//                pre-order partial, or -1 (leaf child, or the child is the next
-//                step j-1 and receives it in registers)
-//   self_slot  : stack slot holding this node's own pre-order partial, or -1
-//                (root, or carried in registers from step j+1)
+//   br[c]      : row of the instance's transition tables for the branch above
+//                child c, equal to the gradient index node.num - 1; index
+//                n_branch is the identity of the zero-length "virtual" branches
+//                that binarise multifurcations (no gradient output)
+//   fpop       : post-order sweep: stack slot holding op[0]'s partial (op[0]
+//                internal), else -1
+//   fpush      : post-order sweep: stack slot this step's partial is pushed to,
+//                or -1 (consumed by step j+1 as op[1], or the root)
+//   bpush      : pre-order sweep: stack slot child 0's pre-order partial is pushed
+//                to (op[0] internal), else -1
+//   bpop       : pre-order sweep: stack slot holding this step's own pre-order
+//                partial, or -1 (the root, or carried from step j+1)
 struct alignas(16) SchedNode {
     int32_t op[2];
     int32_t br[2];
-    int32_t ps[2];
-    int32_t self_slot;
-    int32_t pad;
+    int32_t fpop;
+    int32_t fpush;
+    int32_t bpush;
+    int32_t bpop;
 };
 static_assert(sizeof(SchedNode) == 32, "SchedNode is two 16-byte words");
 
@@ -41,13 +46,14 @@ struct alignas(16) InstanceDesc {
     int32_t n_branch;    // real branches = N-1 (P/dP rows 0..n_branch-1, identity at n_branch)
     int32_t dense;       // 1: leaf partials stored densely, 0: state bitmasks
     int32_t n_blocks;    // S_pad / site block
-    int32_t pre_slots;   // pre-order stack depth of this instance
+    int32_t pre_slots;   // stack depth of this instance (both sweeps)
+    int32_t ambig;       // 1: some leaf code allows more than one but not all states
     int64_t sched_off;   // into the schedule array (SchedNode units)
-    int64_t p_off;       // into the P / dP tables (Real units); rows are [branch][rate][Kp][Kp]
+    int64_t rec_off;     // into the step-record table (bytes); records are [rate][step]
     int64_t leaf_off;    // into the code table (code units) or dense table (Real units)
     int64_t param_off;   // into the FP64 parameter block
     int64_t item_off;    // first work item of this instance
-    int64_t pgrad_off;   // into the per-item gradient partials (float units)
+    int64_t pgrad_off;   // into the per-item gradient partials (Real units)
     int64_t blen_off;    // into the packed branch-length vector
     int64_t grad_off;    // into the packed gradient output
 };
@@ -69,7 +75,7 @@ struct Schedule {
     int32_t J = 0;                 // binary internal schedule nodes
     int32_t n_virtual = 0;         // identity branches added for multifurcations
     int32_t max_depth = 0;
-    int32_t pre_slots = 0;         // depth of the pre-order partial stack
+    int32_t pre_slots = 0;         // depth of the larger of the two partial stacks
     std::vector<SchedNode> nodes;  // post-order, root last
     std::vector<int64_t> leaves;   // leaf nums in the order the schedule expects (sorted)
 };

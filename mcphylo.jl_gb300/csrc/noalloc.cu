@@ -18,7 +18,8 @@
 //     of resident blocks of the fused kernel is reduced until the per-warp
 //     partials fit (fewer blocks: slower, same results);
 //   - every call, from every handle in the process, uses the same array and
-//     leaves its contents behind (only the work counter is cleared per call),
+//     leaves its contents behind (only the work counter and the error flag are
+//     cleared per call; a staging timeout is not reported by this entry point),
 //     so calls whose GPU work overlaps (different streams, different host
 //     threads) race and must be serialised by the caller;
 //   - the first call on a device looks up the array's device address with
@@ -156,30 +157,28 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     unsigned char* s = static_cast<unsigned char*>(base);
     cudaStream_t st = h->stream;
 
-    BuildPArgs b{};
+    BuildRecArgs b{};
     b.inst = static_cast<const InstanceDesc*>(h->d_desc.p);
-    b.rows = static_cast<const int2*>(h->d_rows.p);
-    b.n_rows = int32_t(h->n_prows);
+    b.sched = static_cast<const SchedNode*>(h->d_sched.p);
+    b.steps = static_cast<const int2*>(h->d_steps.p);
+    b.n_steps = int32_t(h->n_steps);
     b.params = static_cast<const double*>(h->d_params.p);
     b.blen = d_blen_packed;
-    b.P = h->d_P.p;
-    b.dP = h->d_dP.p;
+    b.recs = static_cast<unsigned char*>(h->d_recs.p);
     b.K = h->K;
     b.Kp = h->Kp;
     b.C = h->C;
-    b.want_grad = 1;
-    NA_CK(launch_build_p(f64, b, st));
+    NA_CK(launch_build_records(f64, b, st));
 
-    NA_CK(cudaMemsetAsync(s + off_counter, 0, sizeof(int32_t), st));
+    // work counter and error flag start at zero on every call
+    NA_CK(cudaMemsetAsync(s + off_counter, 0, 2 * sizeof(int32_t), st));
     PruneArgs a{};
     a.inst = b.inst;
-    a.sched = static_cast<const SchedNode*>(h->d_sched.p);
     a.items = static_cast<const int2*>(h->d_items.p);
     a.queue = static_cast<const int32_t*>(h->d_queue.p);
     a.n_items = int32_t(h->n_items);
     a.counter = reinterpret_cast<int32_t*>(s + off_counter);
-    a.P = h->d_P.p;
-    a.dP = h->d_dP.p;
+    a.recs = b.recs;
     a.codes = h->d_codes.p;
     a.dense = h->d_dense.p;
     a.params = b.params;

@@ -13,12 +13,14 @@
 // product of the children's contributions, hence logL and every real branch's
 // gradient, is unchanged; only extra power-of-two rescalings are inserted.
 //
-// Because the order is depth-first, the backward sweep (reverse order) consumes
-// stored pre-order partials last-in first-out, so they live in a small stack of
-// slots whose depth is bounded by the tree height.
+// Because the order is depth-first, both sweeps consume stored partials
+// last-in first-out, so they live in small stacks of slots.  Visiting the child
+// with the larger Strahler number first bounds those stacks by the tree's
+// Strahler number (about log4 of the number of leaves for random trees).
 //
-// Children are taken in increasing num order; the reference takes node.children
-// order.  The two only differ in the order of a product, i.e. in rounding.
+// The reference takes children in node.children order; here they are taken by
+// decreasing Strahler number, then increasing num.  The two only differ in the
+// order of a product, i.e. in rounding.
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -53,6 +55,38 @@ std::string build_schedule(int64_t N, const int64_t* parent,
     for (int64_t n = 1; n <= N; ++n)
         if (cptr[n] - cptr[n - 1] == 1)
             return "node " + std::to_string(n) + " has a single child (unary nodes are not supported)";
+
+    // Strahler numbers (children before parents: post-order of the parent array
+    // is not known yet, so iterate to a fixed point over a topological order)
+    std::vector<int32_t> strahler(N, 1);
+    {
+        std::vector<int64_t> order;
+        order.reserve(N);
+        std::vector<int64_t> stk(1, N);
+        std::vector<char> seen(N, 0);
+        while (!stk.empty()) {
+            int64_t n = stk.back();
+            stk.pop_back();
+            if (seen[n - 1]) return "cycle in parent array";
+            seen[n - 1] = 1;
+            order.push_back(n);
+            for (int64_t q = cptr[n - 1]; q < cptr[n]; ++q) stk.push_back(cidx[q]);
+        }
+        for (auto it = order.rbegin(); it != order.rend(); ++it) {
+            const int64_t n = *it;
+            if (cptr[n] == cptr[n - 1]) continue;
+            int32_t best = 0, cnt = 0;
+            for (int64_t q = cptr[n - 1]; q < cptr[n]; ++q) {
+                const int32_t v = strahler[cidx[q] - 1];
+                if (v > best) { best = v; cnt = 1; }
+                else if (v == best) cnt++;
+            }
+            strahler[n - 1] = cnt >= 2 ? best + 1 : best;
+        }
+        for (int64_t n = 1; n <= N; ++n)
+            std::stable_sort(cidx.begin() + cptr[n - 1], cidx.begin() + cptr[n],
+                             [&](int64_t x, int64_t y) { return strahler[x - 1] > strahler[y - 1]; });
+    }
 
     const bool map_leaves = !leaf_row_of_num.empty();
     if (map_leaves && (int64_t)leaf_row_of_num.size() < N) return "leaf map shorter than N";
@@ -115,9 +149,7 @@ std::string build_schedule(int64_t N, const int64_t* parent,
             sn.br[0] = pf.acc_br;
             sn.op[1] = opn;
             sn.br[1] = int32_t(n - 1);
-            sn.ps[0] = sn.ps[1] = -1;
-            sn.self_slot = -1;
-            sn.pad = 0;
+            sn.fpop = sn.fpush = sn.bpush = sn.bpop = -1;
             out.nodes.push_back(sn);
             pf.acc_op = int32_t(out.nodes.size()) - 1;
             pf.acc_br = ident;
@@ -128,26 +160,54 @@ std::string build_schedule(int64_t N, const int64_t* parent,
     if (visited != N) return "parent array is not connected to the root (cycle or forest)";
     out.N = N;
     out.J = int32_t(out.nodes.size());
+    // Canonical operand order: in a depth-first post-order an internal operand
+    // that is the previous step (j-1) can only be the last child folded in, or
+    // the first one when the last is a leaf.  Put it in position 1, so that
+    // "op[1] >= 0" always means "op[1] == j-1" (carried in registers by the kernel).
+    for (int32_t j = 0; j < out.J; ++j) {
+        SchedNode& sn = out.nodes[j];
+        if (sn.op[0] == j - 1 && sn.op[0] >= 0) {
+            std::swap(sn.op[0], sn.op[1]);
+            std::swap(sn.br[0], sn.br[1]);
+        }
+        if (sn.op[1] >= 0 && sn.op[1] != j - 1)
+            return "internal error: schedule is not a depth-first post-order";
+    }
     out.max_depth = max_depth;
     std::sort(out.leaves.begin(), out.leaves.end());
 
-    // Pre-order stack slots.  The backward sweep runs j = J-1 .. 0; at step j the
-    // pre-order partial of each internal child goes to registers if the child is
-    // step j-1, else onto the stack; it is popped when the child's step runs.
+    // Post-order sweep stack: a step's partial is pushed unless step j+1 consumes
+    // it as op[1]; op[0] (never the previous step) is popped.
     std::vector<int32_t> slot_of(out.J, -1);
     int32_t top = 0, max_top = 0;
+    for (int32_t j = 0; j < out.J; ++j) {
+        SchedNode& sn = out.nodes[j];
+        if (sn.op[0] >= 0) {
+            if (slot_of[sn.op[0]] != top - 1) return "internal error: post-order stack is not LIFO";
+            sn.fpop = slot_of[sn.op[0]];
+            --top;
+        }
+        const bool carried = (j + 1 < out.J) && out.nodes[j + 1].op[1] == j;
+        if (j + 1 < out.J && !carried) {
+            sn.fpush = top;
+            slot_of[j] = top++;
+            max_top = std::max(max_top, top);
+        }
+    }
+    // Pre-order sweep stack (j = J-1 .. 0): child 0's pre-order partial is pushed,
+    // child 1's (the next step) stays in registers.
+    std::fill(slot_of.begin(), slot_of.end(), -1);
+    top = 0;
     for (int32_t j = out.J - 1; j >= 0; --j) {
         SchedNode& sn = out.nodes[j];
         if (slot_of[j] >= 0) {
             if (slot_of[j] != top - 1) return "internal error: pre-order stack is not LIFO";
-            sn.self_slot = slot_of[j];
+            sn.bpop = slot_of[j];
             --top;
         }
-        for (int c = 0; c < 2; ++c) {
-            const int32_t o = sn.op[c];
-            if (o < 0 || o == j - 1) continue;
-            sn.ps[c] = top;
-            slot_of[o] = top++;
+        if (sn.op[0] >= 0) {
+            sn.bpush = top;
+            slot_of[sn.op[0]] = top++;
             max_top = std::max(max_top, top);
         }
     }

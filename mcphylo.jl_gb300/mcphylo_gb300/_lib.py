@@ -10,7 +10,8 @@ import ctypes
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libmcphylo_gpu.so")
+# MCPHYLO_GPU_LIB selects another build of the library (same ABI)
+LIB_PATH = os.environ.get("MCPHYLO_GPU_LIB") or os.path.join(_HERE, "libmcphylo_gpu.so")
 
 OK = 0
 ERR_ARG, ERR_SHAPE, ERR_TREE, ERR_OOM, ERR_CUDA, ERR_STATE, ERR_TIMEOUT, ERR_NO_DEVICE, ERR_DATA = (

@@ -229,3 +229,25 @@ def test_full_size_gtr_gamma_f32_vs_f64(built_lib):
     llo, go = oracle(sub)
     ll, g = engine(sub, "f64").logpdf_grad()
     assert abs(ll - llo) <= F64_RTOL * abs(llo)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_partially_ambiguous_codes(built_lib, precision):
+    """0/1 leaf data where some cells allow two or three states (and one allows
+    none) take the kernel's bitmask path; results match the oracle."""
+    inst = random_instance(4, 2, 20, 90, seed=17)
+    rng = np.random.default_rng(4)
+    codes = inst.codes.copy()
+    pick = rng.random(codes.shape) < 0.15
+    codes[pick] |= (np.uint32(1) << rng.integers(0, 4, size=pick.sum()).astype(np.uint32))
+    codes[0, 0] = 0b0110
+    inst2 = simulate.Instance(inst.tree, inst.parent, inst.blen, inst.leaf_nums, codes, inst.U,
+                              inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    llo, go = oracle(inst2)
+    ll, g = engine(inst2, precision).logpdf_grad()
+    if precision == "f64":
+        assert abs(ll - llo) <= F64_RTOL * abs(llo)
+        assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
+    else:
+        assert abs(ll - llo) <= F32_LL_RTOL * abs(llo)
+        assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
