@@ -159,6 +159,15 @@ int mcphy_synchronize(mcphy_handle h);
 /* Launch shape of the fused pruning kernel: sites per thread (1, 2 or 4) and
  * threads per block (64..1024, multiple of 32); 0 keeps the automatic choice. */
 int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block);
+/* Picks the fused kernel's launch shape for the current problem: times each
+ * candidate (sites per thread x threads per block) on full evaluations and keeps
+ * the fastest; out2 (may be NULL) receives it.  No counterpart in the reference
+ * (its @tturbo loops are tuned by LoopVectorization at compile time). */
+int mcphy_autotune(mcphy_handle h, int* out2);
+/* Replays every host-API evaluation as one captured CUDA graph (fused sweep,
+ * reduction and result copies), re-captured when the layout changes.  Per-kernel
+ * timing is not collected while on.  No counterpart in the reference. */
+int mcphy_enable_graph(mcphy_handle h, int on);
 /* Per-call device timing (CUDA events around each kernel of the last evaluation),
  * milliseconds: [0] P/dP build, [1] fused pruning kernel, [2] reduction. */
 int mcphy_enable_timing(mcphy_handle h, int on);
@@ -167,6 +176,11 @@ int mcphy_get_timing(mcphy_handle h, float* ms3);
  * (sum over instances of (N_i-1)*S_i*C), [2] bytes of device scratch in use. */
 int mcphy_get_counts(mcphy_handle h, int64_t* counts3);
 const char* mcphy_last_error(mcphy_handle h);
+/* Test hook, no counterpart in the reference: kind 1 makes the next evaluation's
+ * first staging wait run out (its copy is never issued) so that the bounded-wait
+ * path can be tested without a device fault; that evaluation returns
+ * MCPHY_ERR_TIMEOUT and later ones are unaffected.  kind 0 clears it. */
+int mcphy_debug_inject(mcphy_handle h, int kind);
 const char* mcphy_status_string(int status);
 /* Library version as major*10000 + minor*100 + patch. */
 int mcphy_version(void);

@@ -113,8 +113,17 @@ void choose_tiles(mcphy_engine* h) {
     h->tpb = tpb;
 }
 
+void drop_graphs(mcphy_engine* h) {
+    for (auto& g : h->graph_exec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
 // Rebuilds schedules, offsets, work items and device tables.
 int layout(mcphy_engine* h) {
+    drop_graphs(h);
     choose_tiles(h);
     const int SB = 32 * h->spt;
     const int K = h->K, Kp = h->Kp, C = h->C;
@@ -235,7 +244,7 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_codes, code_bytes * size_t(h->leaf_elems)))) return rc;
     if ((rc = ensure(h, h->d_dense, h->any_dense ? rs * size_t(h->leaf_elems) : 256))) return rc;
     if ((rc = ensure_pinned(h, h->h_blen, h->h_blen_cap, size_t(h->total_branch)))) return rc;
-    if ((rc = ensure_pinned(h, h->h_out, h->h_out_cap, size_t(h->M + h->total_branch)))) return rc;
+    if ((rc = ensure_pinned(h, h->h_out, h->h_out_cap, size_t(h->M + h->total_branch) + 1))) return rc;
 
     CK(cudaMemcpy(h->d_desc.p, h->desc.data(), sizeof(InstanceDesc) * h->M, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_sched.p, h->sched_all.data(), sizeof(SchedNode) * h->sched_all.size(),
@@ -428,6 +437,9 @@ int run(mcphy_engine* h, bool want_grad) {
     a.K = h->K;
     a.C = h->C;
     a.want_grad = want_grad ? 1 : 0;
+    a.wait_limit = h->inject ? 4096 : kWaitLimit;
+    a.inject_timeout = h->inject == 1 ? 1 : 0;
+    h->inject = 0;
     CK(f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
            : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
     if (h->timing) CK(cudaEventRecord(h->ev[2], st));
@@ -457,19 +469,72 @@ int finish_timing(mcphy_engine* h) {
     return MCPHY_OK;
 }
 
+// Enqueues the evaluation and the copies of its results (and of the device error
+// flag) into the pinned output buffer.
+int enqueue_eval(mcphy_engine* h, bool want_grad) {
+    int rc;
+    if ((rc = run(h, want_grad))) return rc;
+    const size_t n = size_t(h->M) + (want_grad ? size_t(h->total_branch) : 0);
+    CK(cudaMemcpyAsync(h->h_out, h->d_out.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->h_out + h->M + h->total_branch, static_cast<int32_t*>(h->d_counter.p) + 1,
+                       sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    return MCPHY_OK;
+}
+
+// Captures enqueue_eval into a CUDA graph (once per layout and mode).
+int graph_for(mcphy_engine* h, bool want_grad, cudaGraphExec_t* out) {
+    cudaGraphExec_t& ex = h->graph_exec[want_grad ? 1 : 0];
+    if (!ex) {
+        const bool timing = h->timing;
+        h->timing = false;
+        // one eager evaluation first, so that every launch-time setting (kernel
+        // attributes) is made outside the capture
+        int rc0 = enqueue_eval(h, want_grad);
+        if (rc0) {
+            h->timing = timing;
+            return rc0;
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_eval(h, want_grad);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        h->timing = timing;
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(h, MCPHY_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ex = nullptr;
+            return fail(h, MCPHY_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+    }
+    *out = ex;
+    return MCPHY_OK;
+}
+
 int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
     if (!h) return MCPHY_ERR_ARG;
     if (!ll) return fail(h, MCPHY_ERR_ARG, "ll is NULL");
     if (want_grad && !grad) return fail(h, MCPHY_ERR_ARG, "grad is NULL");
     int rc;
     if ((rc = prepare(h))) return rc;
-    if ((rc = run(h, want_grad))) return rc;
-    const size_t n = size_t(h->M) + (want_grad ? size_t(h->total_branch) : 0);
-    CK(cudaMemcpyAsync(h->h_out, h->d_out.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(&h->h_flag, static_cast<int32_t*>(h->d_counter.p) + 1, sizeof(int32_t),
-                       cudaMemcpyDeviceToHost, h->stream));
+    int32_t* flag = reinterpret_cast<int32_t*>(h->h_out + h->M + h->total_branch);
+    *flag = 0;
+    if (h->use_graph && !h->timing && !h->inject) {
+        cudaGraphExec_t ex = nullptr;
+        if ((rc = graph_for(h, want_grad, &ex))) return rc;
+        CK(cudaGraphLaunch(ex, h->stream));
+        h->counts[0] = 4;
+        h->counts[1] = h->units;
+    } else {
+        if ((rc = enqueue_eval(h, want_grad))) return rc;
+    }
     CK(cudaStreamSynchronize(h->stream));
-    if (h->h_flag != 0)
+    if (*flag != 0)
         return fail(h, MCPHY_ERR_TIMEOUT, "a bounded wait in the fused kernel gave up (staging of step records)");
     if ((rc = finish_timing(h))) return rc;
     std::memcpy(ll, h->h_out, sizeof(double) * h->M);
@@ -570,6 +635,7 @@ int mcphy_destroy(mcphy_handle h) {
     if (!h) return MCPHY_ERR_ARG;
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graphs(h);
     DevBuf* bufs[] = {&h->d_desc, &h->d_sched, &h->d_items, &h->d_queue, &h->d_steps,
                       &h->d_recs, &h->d_codes, &h->d_dense, &h->d_params, &h->d_blen, &h->d_pgrad,
                       &h->d_pll, &h->d_part, &h->d_out, &h->d_post, &h->d_pre, &h->d_counter};
@@ -836,6 +902,71 @@ int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block)
     h->spt_req = sites_per_thread;
     h->tpb_req = threads_per_block;
     h->dirty |= DIRTY_LAYOUT;
+    return MCPHY_OK;
+}
+
+int mcphy_debug_inject(mcphy_handle h, int kind) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (kind != 0 && kind != 1) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
+    h->inject = kind;
+    return MCPHY_OK;
+}
+
+int mcphy_enable_graph(mcphy_handle h, int on) {
+    if (!h) return MCPHY_ERR_ARG;
+    h->use_graph = on != 0;
+    if (!h->use_graph) drop_graphs(h);
+    return MCPHY_OK;
+}
+
+int mcphy_autotune(mcphy_handle h, int* out2) {
+    if (!h) return MCPHY_ERR_ARG;
+    std::vector<std::pair<int, int>> cand;
+    if (h->prec == MCPHY_PREC_F64)
+        cand = h->Kp <= 4 ? std::vector<std::pair<int, int>>{{1, 128}, {2, 128}, {1, 64}, {2, 64}}
+                          : std::vector<std::pair<int, int>>{{1, 128}, {1, 64}};
+    else if (h->Kp <= 4)
+        cand = {{4, 128}, {4, 64}, {2, 128}, {2, 64}, {4, 256}, {1, 128}};
+    else if (h->Kp <= 8)
+        cand = {{1, 128}, {2, 128}, {1, 64}, {2, 64}};
+    else
+        cand = {{1, 64}, {1, 128}, {1, 32}};
+    const bool timing = h->timing, graph = h->use_graph;
+    h->timing = true;
+    h->use_graph = false;
+    float best = 1e30f;
+    int bs = h->spt_req, bt = h->tpb_req;
+    int rc = MCPHY_OK;
+    std::vector<double> ll(h->M), g(1);
+    for (auto [spt, tpb] : cand) {
+        h->spt_req = spt;
+        h->tpb_req = tpb;
+        h->dirty |= DIRTY_LAYOUT;
+        if ((rc = prepare(h))) break;
+        if (g.size() < size_t(h->total_branch)) g.resize(h->total_branch);
+        float t = 1e30f;
+        for (int rep = 0; rep < 3 && rc == MCPHY_OK; ++rep) {
+            rc = eval_host(h, ll.data(), g.data(), true);
+            if (rep > 0) t = std::min(t, h->ms[1]);
+        }
+        if (rc) break;
+        if (t < best) {
+            best = t;
+            bs = spt;
+            bt = tpb;
+        }
+    }
+    h->timing = timing;
+    h->use_graph = graph;
+    h->spt_req = bs;
+    h->tpb_req = bt;
+    h->dirty |= DIRTY_LAYOUT;
+    if (rc) return rc;
+    if ((rc = prepare(h))) return rc;
+    if (out2) {
+        out2[0] = h->spt;
+        out2[1] = h->tpb;
+    }
     return MCPHY_OK;
 }
 

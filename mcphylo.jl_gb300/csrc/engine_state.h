@@ -81,8 +81,13 @@ struct mcphy_engine {
 
     double* h_blen = nullptr;
     size_t h_blen_cap = 0;
-    double* h_out = nullptr;
+    double* h_out = nullptr;      // pinned: [ll (M) | grad (total_branch) | error flag]
     int32_t h_flag = 0;
+    // test hook: make the next evaluation's first staging wait run out
+    int inject = 0;
+    // CUDA graph replay of a whole evaluation (fused sweep + reduction + copies)
+    bool use_graph = false;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // [logL only, logL + gradient]
     size_t h_out_cap = 0;
 
     bool timing = false;

@@ -102,6 +102,8 @@ struct PruneArgs {
     int32_t K;
     int32_t C;
     int32_t want_grad;
+    int32_t wait_limit;       // iterations of every bounded mbarrier wait
+    int32_t inject_timeout;   // test hook: never issue the first staging copy
 };
 
 struct BuildRecArgs {
@@ -291,9 +293,9 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 }
 // Bounded wait for the phase with the given parity; false if it never completed.
 constexpr int kWaitLimit = 1 << 22;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit = kWaitLimit) {
     const uint32_t a = smem_u32(bar);
-    for (int it = 0; it < kWaitLimit; ++it) {
+    for (int it = 0; it < limit; ++it) {
         uint32_t ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -319,13 +321,17 @@ struct Stage {
     const unsigned char* tsrc;  // leaf codes of the current (instance, site block), or null
     int J;
     int Q;                      // chunks
+    int limit;                  // bounded-wait iterations
+    bool skip_first;            // test hook: chunk 0 is never issued
     bool ok;
 
     __device__ uint64_t* barrier(int b) const { return bars + b; }
-    __device__ void init(unsigned char* p, uint64_t* b, int lane) {
+    __device__ void init(unsigned char* p, uint64_t* b, int lane, int wait_limit, bool skip) {
         base = p;
         bars = b;
         parity = 0u;
+        limit = wait_limit;
+        skip_first = skip;
         ok = true;
         if (lane == 0) {
             mbar_init(barrier(0), 1);
@@ -335,7 +341,7 @@ struct Stage {
     // Lane 0 starts chunk x into its buffers; the warp must have finished reading
     // them (__syncwarp before).
     __device__ void issue(int x, int lane) {
-        if (lane == 0) {
+        if (lane == 0 && !(skip_first && x == 0)) {
             const int first = x * CH;
             const int n = min(CH, J - first);
             const int b = x & 1;
@@ -357,7 +363,7 @@ struct Stage {
     // Waits for chunk x (the next phase of its buffer).  Warp-uniform result.
     __device__ bool wait(int x) {
         const int b = x & 1;
-        bool done = mbar_wait(barrier(b), (parity >> b) & 1u);
+        bool done = mbar_wait(barrier(b), (parity >> b) & 1u, limit);
         done = __all_sync(0xffffffffu, done);
         if (done) parity ^= (1u << b);
         ok = ok && done;
@@ -542,7 +548,7 @@ prune_kernel(const PruneArgs a) {
     uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
                                                   NS * SLOT * sizeof(Real));
     St st;
-    st.init(wbase, bars, lane);
+    st.init(wbase, bars, lane, a.wait_limit, a.inject_timeout != 0);
     if (lane == 0) fence_mbar_init();
     __syncwarp();
     // stack slot s: shared memory below NS, the warp's global column above
@@ -749,8 +755,8 @@ prune_kernel(const PruneArgs a) {
         // a bounded wait gave up: report, and let the copies this warp issued land
         // (bounded as well) before its shared memory is released
         if (lane == 0) atomicExch(a.counter + 1, 1);
-        mbar_wait(st.barrier(0), st.parity & 1u);
-        mbar_wait(st.barrier(1), (st.parity >> 1) & 1u);
+        mbar_wait(st.barrier(0), st.parity & 1u, a.wait_limit);
+        mbar_wait(st.barrier(1), (st.parity >> 1) & 1u, a.wait_limit);
     }
 }
 

@@ -1,4 +1,6 @@
 // FP32-scaled instantiations of the fused pruning kernel.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace mcphy {
@@ -6,9 +8,14 @@ namespace mcphy {
 template <int KP, int SPT>
 static cudaError_t go(int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
     const int smem = (tpb / 32) * warp_smem_bytes(KP, SPT, int(sizeof(float)));
-    cudaError_t e = cudaFuncSetAttribute(prune_kernel<KP, float, SPT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
+    // the attribute is set once per launch shape (not inside a stream capture)
+    static int set_for = 0;
+    if (set_for < smem) {
+        cudaError_t e = cudaFuncSetAttribute(prune_kernel<KP, float, SPT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        set_for = smem;
+    }
     prune_kernel<KP, float, SPT><<<blocks, tpb, smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -43,7 +50,10 @@ cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, int* bps) {
     const void* f = pick(Kp, spt);
     if (!f) return cudaErrorInvalidValue;
     const int smem = (tpb / 32) * warp_smem_bytes(Kp, spt, int(sizeof(float)));
-    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // the largest shape any later launch may use, so launches need not set it again
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         std::max(smem, 8 * warp_smem_bytes(Kp, spt, int(sizeof(float)))));
+    if (e != cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, f, tpb, smem);
 }

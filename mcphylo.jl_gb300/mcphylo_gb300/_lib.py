@@ -56,6 +56,9 @@ SIGNATURES = {
     "mcphy_set_stream": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_synchronize": (c_int, [handle_t]),
     "mcphy_set_tiles": (c_int, [handle_t, c_int, c_int]),
+    "mcphy_autotune": (c_int, [handle_t, P(c_int)]),
+    "mcphy_enable_graph": (c_int, [handle_t, c_int]),
+    "mcphy_debug_inject": (c_int, [handle_t, c_int]),
     "mcphy_enable_timing": (c_int, [handle_t, c_int]),
     "mcphy_get_timing": (c_int, [handle_t, P(ctypes.c_float)]),
     "mcphy_get_counts": (c_int, [handle_t, pi64]),

@@ -131,6 +131,18 @@ class Engine:
         check(self._L.mcphy_set_tiles(self._h, sites_per_thread, threads_per_block), self._h,
               "set_tiles")
 
+    def autotune(self):
+        """Time the candidate launch shapes on the current problem; keep the fastest."""
+        out = (ctypes.c_int * 2)()
+        check(self._L.mcphy_autotune(self._h, out), self._h, "autotune")
+        return int(out[0]), int(out[1])
+
+    def enable_graph(self, on: bool = True) -> None:
+        check(self._L.mcphy_enable_graph(self._h, 1 if on else 0), self._h)
+
+    def debug_inject(self, kind: int) -> None:
+        check(self._L.mcphy_debug_inject(self._h, int(kind)), self._h)
+
     def set_stream(self, stream_ptr: int) -> None:
         check(self._L.mcphy_set_stream(self._h, ctypes.c_void_p(stream_ptr or None)), self._h)
 

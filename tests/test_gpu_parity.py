@@ -251,3 +251,46 @@ def test_partially_ambiguous_codes(built_lib, precision):
     else:
         assert abs(ll - llo) <= F32_LL_RTOL * abs(llo)
         assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
+
+
+def test_bounded_wait_timeout_is_reported_and_recoverable(built_lib):
+    """A staging wait that nothing completes (test hook) ends with
+    MCPHY_ERR_TIMEOUT instead of a hang; the context stays usable."""
+    inst = random_instance(4, 2, 30, 300, seed=41)
+    e = engine(inst, "f32")
+    ll0, g0 = e.logpdf_grad()
+    e.debug_inject(1)
+    with pytest.raises(mp.MCPhyError) as ei:
+        e.logpdf_grad()
+    assert ei.value.status == -7
+    ll1, g1 = e.logpdf_grad()
+    assert ll1 == ll0 and np.array_equal(g1, g0)
+
+
+def test_graph_replay_matches_eager(built_lib):
+    inst = random_instance(4, 4, 40, 700, seed=43)
+    e = engine(inst, "f32")
+    ref = e.logpdf_grad()
+    e.enable_graph(True)
+    rng = np.random.default_rng(1)
+    for _ in range(3):
+        a = e.logpdf_grad()
+        assert a[0] == ref[0] and np.array_equal(a[1], ref[1])
+    b2 = inst.blen * rng.uniform(0.8, 1.2, size=inst.blen.shape)
+    e.set_branch_lengths(b2)
+    got = e.logpdf_grad()
+    assert e.logpdf() == got[0]
+    e.enable_graph(False)
+    want = e.logpdf_grad()
+    assert got[0] == want[0] and np.array_equal(got[1], want[1])
+
+
+def test_autotune_keeps_results(built_lib):
+    inst = random_instance(4, 4, 50, 2000, seed=45)
+    e = engine(inst, "f32")
+    ll0, g0 = e.logpdf_grad()
+    spt, tpb = e.autotune()
+    assert spt in (1, 2, 4) and tpb in (64, 128, 256)
+    ll1, g1 = e.logpdf_grad()
+    assert abs(ll1 - ll0) <= 1e-9 * abs(ll0)
+    assert_grad_close(g1, g0, 1e-5, F32_G_FLOOR)
