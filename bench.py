@@ -246,6 +246,133 @@ def run_reference(args, rank, world):
     return 0
 
 
+# ----------------------------------------------------------------------------- NUTS ESS/s
+NUTS_PRIOR = (1.0, 1.0, 0.1, 1.0)     # CompoundDirichlet(alpha, a, beta, c)
+
+
+def _oracle_posterior(inst, prior):
+    from oracle import pyoracle as O
+    x = np.asfortranarray(inst.tensor())
+    model = (inst.U, inst.D, inst.Uinv, inst.mu)
+    timer = {"grad_s": 0.0, "grad_n": 0, "logf_s": 0.0, "logf_n": 0}
+
+    def lfg(p, b):
+        t0 = time.perf_counter()
+        ll, g = O.gradlogpdf(O.tree_from_parent(p, b), x, inst.pi, model, inst.rates)
+        timer["grad_s"] += time.perf_counter() - t0
+        timer["grad_n"] += 1
+        lp, gp = prior.logpdf_grad(p, b)
+        return ll + lp, g + gp
+
+    def lf(p, b):
+        t0 = time.perf_counter()
+        ll = O.logpdf(O.tree_from_parent(p, b), x, inst.pi, model, inst.rates)
+        timer["logf_s"] += time.perf_counter() - t0
+        timer["logf_n"] += 1
+        return ll + prior.logpdf_grad(p, b)[0]
+
+    return lfg, lf, timer
+
+
+def _chain_summary(ch):
+    e = ch.ess()
+    ess_min = min(e["logf"], e["tree_length"])
+    return {"ess_per_s": ess_min / ch.seconds, "ess": e, "seconds": round(ch.seconds, 3),
+            "iterations": len(ch.logf), "grad_evals": ch.grad_evals,
+            "logf_evals": ch.logf_evals, "mean_depth": float(np.mean(ch.depth)),
+            "epsilon": ch.epsilon, "nni_moves": int(np.sum(ch.nni_moves)),
+            "ms_per_grad_eval": 1e3 * ch.seconds / max(ch.grad_evals, 1),
+            "adapt_seconds": round(ch.adapt_seconds, 3)}
+
+
+def run_nuts(args):
+    """NUTS ESS/s: one PNUTS chain over the branch lengths of one workload (the
+    likelihood times a CompoundDirichlet(1, 1, 0.1, 1) tree prior), driven by the
+    FP32 engine, by the FP64 engine and by the CPU oracle with the same seed.
+    ESS = min over (log posterior, tree length) of min((SD / MCSE_bm)^2, n),
+    batch size 100, over the post-adaptation draws; time = wall clock of those
+    iterations (host sampler + evaluations)."""
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from mcphylo_gb300 import pnuts as P
+    insts, cfg = make_workload(args.workload, workers=min(16, os.cpu_count() or 1))
+    if len(insts) != 1:
+        raise SystemExit("--mode nuts runs on a single-tree workload")
+    inst = insts[0]
+    prior = P.CompoundDirichlet(*NUTS_PRIOR)
+    n_iter, n_adapt = args.nuts_iter, args.nuts_adapt
+    res = {}
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for prec in ("f32", "f64"):
+            post = P.engine_posterior(inst.parent, inst.blen, inst.codes, inst.leaf_nums,
+                                      (inst.U, inst.D, inst.Uinv, inst.mu), inst.pi, inst.rates,
+                                      prior, precision=prec)
+            spent = {"s": 0.0, "n": 0}
+
+            def timed(fn):
+                def call(p, b):
+                    t0 = time.perf_counter()
+                    try:
+                        return fn(p, b)
+                    finally:
+                        spent["s"] += time.perf_counter() - t0
+                        spent["n"] += 1
+                return call
+
+            ch = P.run_chain(inst.parent, inst.blen, timed(post.logfgrad), timed(post.logf),
+                             n_iter=n_iter, n_adapt=n_adapt, seed=args.nuts_seed,
+                             target=args.nuts_target)
+            res[prec] = _chain_summary(ch)
+            res[prec]["set_tree_calls"] = post.n_set_tree
+            # host time of the sampling iterations: wall time minus the evaluations
+            per_eval = spent["s"] / max(spent["n"], 1)
+            res[prec]["host_seconds"] = max(
+                ch.seconds - per_eval * (ch.grad_evals + ch.logf_evals), 0.0)
+    clocks = clk.summary()
+    # CPU: the oracle drives the same sampler.  With the same seed its chain retraces
+    # the FP64 engine's (the decisions agree), so where a full run does not fit the
+    # time budget, its time is the FP64 chain's evaluation counts at the oracle's
+    # measured cost per evaluation plus the FP64 chain's host time.
+    from oracle import pyoracle as O
+    O.lib()
+    lfg, lf, timer = _oracle_posterior(inst, prior)
+    lfg(inst.parent, inst.blen)
+    per_grad = timer["grad_s"]
+    f64 = res["f64"]
+    evals_per_iter = (f64["grad_evals"] + f64["logf_evals"]) / max(n_iter, 1)
+    est_total = (n_iter + n_adapt) * evals_per_iter * per_grad
+    if est_total <= args.cpu_seconds * 4:
+        ch = P.run_chain(inst.parent, inst.blen, lfg, lf, n_iter=n_iter, n_adapt=n_adapt,
+                         seed=args.nuts_seed, target=args.nuts_target)
+        cpu = _chain_summary(ch)
+        cpu["kind"] = "port, full chain"
+    else:
+        timer.update(grad_s=0.0, grad_n=0, logf_s=0.0, logf_n=0)
+        while timer["grad_s"] + timer["logf_s"] < args.cpu_seconds:
+            lfg(inst.parent, inst.blen)
+            lf(inst.parent, inst.blen)
+        g_s = timer["grad_s"] / timer["grad_n"]
+        f_s = timer["logf_s"] / timer["logf_n"]
+        secs = f64["grad_evals"] * g_s + f64["logf_evals"] * f_s + f64["host_seconds"]
+        ess_min = min(f64["ess"]["logf"], f64["ess"]["tree_length"])
+        cpu = {"ess_per_s": ess_min / secs, "seconds": round(secs, 3),
+               "oracle_grad_s": g_s, "oracle_logf_s": f_s,
+               "kind": "port, estimated: the FP64 chain's evaluation counts x the oracle's "
+                       "time per evaluation (%d grad, %d logf evaluations timed) + the FP64 "
+                       "chain's wall time" % (timer["grad_n"], timer["logf_n"])}
+    cpu["cores"] = O.num_threads()
+    out = {"metric": "NUTS ESS/s (PNUTS over branch lengths)", "value": res["f32"]["ess_per_s"],
+           "unit": "effective samples/s", "n_gpus": 1, "higher_is_better": True,
+           "dtype": "f32", "data": "synthetic (seeded simulation)",
+           "config": dict(cfg, iterations=n_iter, adaptation=n_adapt,
+                          prior="CompoundDirichlet(1,1,0.1,1)", target=args.nuts_target,
+                          tree_depth=10, seed=args.nuts_seed),
+           "nuts": {"f32": res["f32"], "f64": res["f64"], "cpu_oracle": cpu},
+           "clocks": clocks}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 # ----------------------------------------------------------------------------- GPU arm
 def autotune(insts, steps=2):
     """Sites per thread x threads per block of the fused kernel, best device time."""
@@ -494,8 +621,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-hky-g4")
     ap.add_argument("--tiles", default="auto", help="auto or SPTxTPB, e.g. 2x256")
-    ap.add_argument("--mode", default="grad", choices=["grad", "logl"],
-                    help="grad: logL + gradient (the headline metric); logl: logL only")
+    ap.add_argument("--mode", default="grad", choices=["grad", "logl", "nuts"],
+                    help="grad: logL + gradient (the headline metric); logl: logL only; "
+                         "nuts: PNUTS ESS/s on a single-tree workload")
+    ap.add_argument("--nuts-iter", type=int, default=1000)
+    ap.add_argument("--nuts-adapt", type=int, default=200)
+    ap.add_argument("--nuts-seed", type=int, default=1)
+    ap.add_argument("--nuts-target", type=float, default=0.8)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -510,6 +642,8 @@ def main():
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.mode == "nuts":
+        return run_nuts(args) if rank == 0 else 0
     return run_gpu(args, rank, world)
 
 
