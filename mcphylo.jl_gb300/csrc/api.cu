@@ -140,8 +140,11 @@ int layout(mcphy_engine* h) {
     int64_t sched_off = 0, rec_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
             pgrad_off = 0, blen_off = 0, nsteps = 0;
     const int64_t psize = param_size(K, Kp, C);
+    int64_t lc_off = 0;
+    h->lc_off.assign(h->M, 0);
     for (int64_t i = 0; i < h->M; ++i) {
         Inst& in = h->inst[i];
+        in.topo_dirty = false;
         if (in.data_N != in.N)
             return fail(h, MCPHY_ERR_SHAPE,
                         "instance " + std::to_string(i) + ": data has " + std::to_string(in.data_N) +
@@ -179,6 +182,10 @@ int layout(mcphy_engine* h) {
         // code leaves: the leaf codes arranged in schedule order, [block][step][operand][32*spt]
         // (internal operands leave their entries unused); dense leaves: [row][S_pad][Kp]
         leaf_off += in.dense ? int64_t(d.n_leaf) * d.S_pad * Kp : int64_t(sc.J) * 2 * d.S_pad;
+        // and, for code leaves, a leaf-major copy [row][S_pad] that the schedule-ordered
+        // table is gathered from on the device (again after a topology change)
+        h->lc_off[i] = lc_off;
+        if (!in.dense) lc_off += int64_t(d.n_leaf) * d.S_pad;
         param_off += psize;
         const int64_t items = int64_t(C) * d.n_blocks;
         item_off += items;
@@ -197,6 +204,7 @@ int layout(mcphy_engine* h) {
     h->n_steps = nsteps;
     h->rec_bytes_total = rec_off;
     h->leaf_elems = leaf_off;
+    h->leafcode_elems = lc_off;
     if (h->n_items >= (int64_t(1) << 31)) return fail(h, MCPHY_ERR_ARG, "too many work items");
 
     // work items and the order warps take them: largest trees first
@@ -242,6 +250,8 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_counter, 256))) return rc;
     const size_t code_bytes = (Kp <= 8) ? 1 : 4;
     if ((rc = ensure(h, h->d_codes, code_bytes * size_t(h->leaf_elems)))) return rc;
+    if ((rc = ensure(h, h->d_leafcodes, code_bytes * size_t(std::max<int64_t>(h->leafcode_elems, 64)))))
+        return rc;
     if ((rc = ensure(h, h->d_dense, h->any_dense ? rs * size_t(h->leaf_elems) : 256))) return rc;
     if ((rc = ensure_pinned(h, h->h_blen, h->h_blen_cap, size_t(h->total_branch)))) return rc;
     if ((rc = ensure_pinned(h, h->h_out, h->h_out_cap, size_t(h->M + h->total_branch) + 1))) return rc;
@@ -277,7 +287,27 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_pre, pre_b))) return rc;
     h->counts[2] = int64_t(post_b + pre_b);
     h->dirty |= DIRTY_DATA | DIRTY_BLEN | DIRTY_MODEL;
-    h->dirty &= ~unsigned(DIRTY_LAYOUT);
+    h->dirty &= ~unsigned(DIRTY_LAYOUT | DIRTY_TOPO);
+    return MCPHY_OK;
+}
+
+// Launches the device gather that fills instance i's schedule-ordered leaf codes
+// from its leaf-major copy (code leaves only).
+int gather_instance(mcphy_engine* h, int64_t i) {
+    const InstanceDesc& d = h->desc[i];
+    if (h->inst[i].dense) return MCPHY_OK;
+    const int cb = (h->Kp <= 8) ? 1 : 4;
+    GatherArgs g{};
+    g.sched = static_cast<const SchedNode*>(h->d_sched.p) + d.sched_off;
+    g.src = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(h->d_leafcodes.p) +
+                                              size_t(h->lc_off[i]) * cb);
+    g.dst = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(h->d_codes.p) +
+                                        size_t(d.leaf_off) * cb);
+    g.J = d.J;
+    g.n_blocks = d.n_blocks;
+    g.slot_words = 32 * h->spt * cb / 4;
+    g.row_words = int64_t(d.S_pad) * cb / 4;
+    CK(launch_gather_codes(g, h->stream));
     return MCPHY_OK;
 }
 
@@ -285,12 +315,11 @@ int upload_data(mcphy_engine* h) {
     const int K = h->K, Kp = h->Kp;
     const uint32_t allmask = (K == 32) ? 0xffffffffu : ((1u << K) - 1u);
     const bool f64 = h->prec == MCPHY_PREC_F64;
-    const int SB = 32 * h->spt;
     std::vector<uint8_t> c8;
     std::vector<uint32_t> c32;
     std::vector<float> df;
     std::vector<double> dd;
-    if (Kp <= 8) c8.assign(h->leaf_elems, 0); else c32.assign(h->leaf_elems, 0);
+    if (Kp <= 8) c8.assign(h->leafcode_elems, 0); else c32.assign(h->leafcode_elems, 0);
     if (h->any_dense) {
         if (f64) dd.assign(h->leaf_elems, 0.0); else df.assign(h->leaf_elems, 0.f);
     }
@@ -317,32 +346,74 @@ int upload_data(mcphy_engine* h) {
                 }
             continue;
         }
-        // leaf codes in schedule order: entry (block, step j, operand c) holds the
-        // codes of the block's sites for the leaf that is operand c of step j
-        const SchedNode* sn = h->sched_all.data() + d.sched_off;
-        for (int j = 0; j < d.J; ++j)
-            for (int c = 0; c < 2; ++c) {
-                if (sn[j].op[c] >= 0) continue;
-                const int64_t row = -int64_t(sn[j].op[c]) - 1;
-                const uint32_t* src = in.codes.data() + row * in.S;
-                for (int64_t b = 0; b < d.n_blocks; ++b) {
-                    const int64_t o = d.leaf_off + ((b * d.J + j) * 2 + c) * SB;
-                    for (int t = 0; t < SB; ++t) {
-                        const int64_t s = b * SB + t;
-                        const uint32_t v = (s < in.S) ? src[s] : allmask;
-                        if (Kp <= 8) c8[o + t] = uint8_t(v); else c32[o + t] = v;
-                    }
-                }
+        // leaf-major codes, padded sites allow every state
+        for (int64_t l = 0; l < d.n_leaf; ++l) {
+            const uint32_t* src = in.codes.data() + l * in.S;
+            const int64_t o = h->lc_off[i] + l * d.S_pad;
+            for (int64_t s = 0; s < d.S_pad; ++s) {
+                const uint32_t v = (s < in.S) ? src[s] : allmask;
+                if (Kp <= 8) c8[o + s] = uint8_t(v); else c32[o + s] = v;
             }
+        }
     }
-    if (Kp <= 8) CK(cudaMemcpy(h->d_codes.p, c8.data(), c8.size(), cudaMemcpyHostToDevice));
-    else CK(cudaMemcpy(h->d_codes.p, c32.data(), c32.size() * 4, cudaMemcpyHostToDevice));
+    const int cb = (Kp <= 8) ? 1 : 4;
+    if (h->leafcode_elems > 0) {
+        CK(cudaMemcpy(h->d_leafcodes.p, Kp <= 8 ? static_cast<const void*>(c8.data()) : c32.data(),
+                      size_t(h->leafcode_elems) * cb, cudaMemcpyHostToDevice));
+        CK(cudaMemsetAsync(h->d_codes.p, 0, size_t(h->leaf_elems) * cb, h->stream));
+    }
     if (h->any_dense) {
         if (f64) CK(cudaMemcpy(h->d_dense.p, dd.data(), dd.size() * 8, cudaMemcpyHostToDevice));
         else CK(cudaMemcpy(h->d_dense.p, df.data(), df.size() * 4, cudaMemcpyHostToDevice));
     }
     CK(cudaMemcpy(h->d_desc.p, h->desc.data(), sizeof(InstanceDesc) * h->M, cudaMemcpyHostToDevice));
+    // leaf codes in schedule order: entry (block, step j, operand c) holds the codes of
+    // the block's sites for the leaf that is operand c of step j
+    int rc;
+    for (int64_t i = 0; i < h->M; ++i)
+        if ((rc = gather_instance(h, i))) return rc;
     h->dirty &= ~unsigned(DIRTY_DATA);
+    return MCPHY_OK;
+}
+
+// A new topology on the same nodes and leaves: rebuild the instance's schedule,
+// upload it and re-gather its leaf codes on the device.  Buffers, launch shape and
+// captured graphs stay valid; a schedule whose step count or stack depth no
+// longer fits the layout falls back to a full layout.
+int retopo(mcphy_engine* h) {
+    std::vector<std::pair<int64_t, Schedule>> todo;
+    for (int64_t i = 0; i < h->M; ++i) {
+        Inst& in = h->inst[i];
+        if (!in.topo_dirty) continue;
+        std::vector<int32_t> row_of(in.N, -1);
+        for (size_t l = 0; l < in.leaf_nums.size(); ++l) row_of[in.leaf_nums[l] - 1] = int32_t(l);
+        Schedule sc;
+        std::string e = build_schedule(in.N, in.parent.data(), row_of, sc);
+        const InstanceDesc& d = h->desc[i];
+        if (!e.empty() || sc.J != d.J || sc.pre_slots > h->max_pre ||
+            sc.leaves.size() != in.leaf_nums.size()) {
+            h->dirty |= DIRTY_LAYOUT;       // errors are reported by the full layout
+            return MCPHY_OK;
+        }
+        todo.emplace_back(i, std::move(sc));
+    }
+    int rc;
+    for (auto& t : todo) {
+        const int64_t i = t.first;
+        InstanceDesc& d = h->desc[i];
+        std::copy(t.second.nodes.begin(), t.second.nodes.end(), h->sched_all.begin() + d.sched_off);
+        d.pre_slots = t.second.pre_slots;
+        CK(cudaMemcpyAsync(static_cast<SchedNode*>(h->d_sched.p) + d.sched_off,
+                           h->sched_all.data() + d.sched_off, sizeof(SchedNode) * size_t(d.J),
+                           cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(static_cast<InstanceDesc*>(h->d_desc.p) + i, &h->desc[i],
+                           sizeof(InstanceDesc), cudaMemcpyHostToDevice, h->stream));
+        if ((rc = gather_instance(h, i))) return rc;
+        h->inst[i].topo_dirty = false;
+    }
+    // pageable sources: make sure the copies have read them before the host moves on
+    CK(cudaStreamSynchronize(h->stream));
+    h->dirty &= ~unsigned(DIRTY_TOPO);
     return MCPHY_OK;
 }
 
@@ -385,6 +456,10 @@ int prepare(mcphy_engine* h) {
     }
     CK(cudaSetDevice(h->device));
     int rc;
+    // a topology change alone re-gathers on the device; retopo() asks for a full
+    // layout when the new schedule does not fit the current one
+    if ((h->dirty & DIRTY_TOPO) && !(h->dirty & DIRTY_LAYOUT))
+        if ((rc = retopo(h))) return rc;
     if (h->dirty & DIRTY_LAYOUT)
         if ((rc = layout(h))) return rc;
     if (h->dirty & DIRTY_DATA)
@@ -742,11 +817,20 @@ int mcphy_batch_set_tree(mcphy_handle h, int64_t i, int64_t nnodes, const int64_
     if (!blen && (!in.has_tree || in.N != nnodes))
         return fail(h, MCPHY_ERR_ARG, "blen is NULL and no lengths of this size are set");
     if (blen && !all_finite(blen, nnodes - 1)) return fail(h, MCPHY_ERR_DATA, "non-finite branch length");
+    // same node count with a layout in place: only the schedule changes (an NNI or
+    // SPR move); anything else is a new layout
+    const bool same_nodes = in.has_tree && in.N == nnodes && !(h->dirty & DIRTY_LAYOUT) &&
+                            !h->desc.empty();
     in.N = nnodes;
     in.parent.assign(parent, parent + nnodes);
     if (blen) in.blen.assign(blen, blen + nnodes - 1);
     in.has_tree = true;
-    h->dirty |= DIRTY_LAYOUT | DIRTY_BLEN;
+    if (same_nodes) {
+        in.topo_dirty = true;
+        h->dirty |= DIRTY_TOPO | DIRTY_BLEN;
+    } else {
+        h->dirty |= DIRTY_LAYOUT | DIRTY_BLEN;
+    }
     return MCPHY_OK;
 }
 

@@ -23,6 +23,7 @@ struct Inst {
     std::vector<int64_t> parent;
     std::vector<double> blen;
     bool has_tree = false;
+    bool topo_dirty = false;   // new topology, same nodes: schedule rebuilt at the next call
     // data
     int64_t S = 0;
     int64_t data_N = 0;
@@ -72,11 +73,13 @@ struct mcphy_engine {
     int64_t pre_warp_stride = 0;
     int32_t max_pre = 0;
     int64_t leaf_elems = 0;
+    int64_t leafcode_elems = 0;       // leaf-major code copy (code units)
+    std::vector<int64_t> lc_off;      // per instance, into d_leafcodes
     bool any_dense = false;
     std::vector<SchedNode> sched_all;
 
     DevBuf d_desc, d_sched, d_items, d_queue, d_steps, d_recs, d_codes, d_dense, d_params,
-        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter;
+        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter, d_leafcodes;
     int n_split = 1;
 
     double* h_blen = nullptr;

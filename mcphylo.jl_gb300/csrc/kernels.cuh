@@ -860,4 +860,22 @@ cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, int* blocks_per_sm);
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st);
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st);
 
+// ---------------------------------------------------------------- leaf-code gather
+// Rebuilds one instance's schedule-ordered leaf codes from its leaf-major copy
+// after the schedule changed (a new topology on the same leaves).  In 32-bit
+// words: slot (block b, step j, operand c) of `slot_words` words at
+// ((b*J + j)*2 + c)*slot_words receives words [b*slot_words, +slot_words) of
+// leaf row r = -op[c]-1, which starts at r*row_words; internal operands' slots
+// are left as they are.
+struct GatherArgs {
+    const SchedNode* sched;   // the instance's J schedule nodes
+    const uint32_t* src;      // leaf-major codes [row][S_pad]
+    uint32_t* dst;            // schedule-ordered codes [block][step][operand][site block]
+    int32_t J;
+    int32_t n_blocks;
+    int32_t slot_words;       // site block x code bytes / 4
+    int64_t row_words;        // S_pad x code bytes / 4
+};
+cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st);
+
 }  // namespace mcphy

@@ -1,4 +1,6 @@
-// Transition-matrix build and the deterministic reduction.
+// Transition-matrix build, the deterministic reduction and the leaf-code gather.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace mcphy {
@@ -85,6 +87,32 @@ cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t s
         build_records_kernel<double><<<unsigned(blocks), tpb, 0, st>>>(a);
     else
         build_records_kernel<float><<<unsigned(blocks), tpb, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) gather_codes_kernel(const GatherArgs a) {
+    const int64_t total = int64_t(a.n_blocks) * a.J * 2 * a.slot_words;
+    for (int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+         idx += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t slot = idx / a.slot_words;
+        const int w = int(idx - slot * a.slot_words);
+        const int c = int(slot & 1);
+        const int64_t jb = slot >> 1;
+        const int64_t b = jb / a.J;
+        const int j = int(jb - b * a.J);
+        const int32_t op = a.sched[j].op[c];
+        if (op >= 0) continue;
+        const int64_t row = -int64_t(op) - 1;
+        a.dst[idx] = __ldg(a.src + row * a.row_words + b * a.slot_words + w);
+    }
+}
+
+cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st) {
+    const int64_t total = int64_t(a.n_blocks) * a.J * 2 * a.slot_words;
+    if (total == 0) return cudaSuccess;
+    const int tpb = 256;
+    const int64_t blocks = std::min<int64_t>((total + tpb - 1) / tpb, 152 * 16);
+    gather_codes_kernel<<<unsigned(blocks), tpb, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -67,6 +67,7 @@ enum DirtyBits : unsigned {
     DIRTY_DATA = 2u,     // leaf tables changed
     DIRTY_BLEN = 4u,     // branch lengths changed
     DIRTY_MODEL = 8u,    // eigensystem / pi / rates changed
+    DIRTY_TOPO = 16u,    // a topology changed on the same nodes and leaves (schedule only)
 };
 
 // Result of turning a parent array into a kernel schedule.

@@ -98,7 +98,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     }
     // Everything but the branch lengths (which come from d_blen_packed) must be on
     // the device already: setters upload and allocate at the next regular call.
-    if (h->dirty & (DIRTY_LAYOUT | DIRTY_DATA | DIRTY_MODEL)) {
+    if (h->dirty & (DIRTY_LAYOUT | DIRTY_DATA | DIRTY_MODEL | DIRTY_TOPO)) {
         h->err = "tree, data or model changed since the last evaluation: call "
                  "mcphy_logpdf_grad (or mcphy_batch_logpdf_grad) once first; this entry "
                  "point neither allocates nor uploads";

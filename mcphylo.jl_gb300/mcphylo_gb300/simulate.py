@@ -56,6 +56,9 @@ def birth_death_tree(n_taxa: int, rng: np.random.Generator, lam: float = 1.0, mu
                 nd.name = "extinct"
         if len(alive) == n_taxa:
             break
+    # observe the tree one waiting time after the last event, so that no tip
+    # born in it has length zero
+    t += rng.exponential(1.0 / ((lam + mu) * n_taxa))
     for nd in alive:
         nd.inc_length = t - birth[id(nd)]
     # prune extinct tips and suppress unary nodes

@@ -173,6 +173,90 @@ def test_branch_lengths_and_topology_updates(built_lib):
     assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
 
 
+def _nni(parent, rng):
+    """A random NNI (child of an internal non-root node <-> that node's sibling)."""
+    N = len(parent)
+    while True:
+        t = int(rng.integers(1, N))
+        kids = np.flatnonzero(parent == t) + 1
+        p = parent[t - 1]
+        sibs = [s for s in np.flatnonzero(parent == p) + 1 if s != t]
+        if len(kids) and p and sibs:
+            q = parent.copy()
+            c, s = int(rng.choice(kids)), int(rng.choice(sibs))
+            q[c - 1], q[s - 1] = p, t
+            return q
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_topology_moves_on_a_live_engine(built_lib, precision):
+    """A new topology on the same nodes (NNI, or moving a leaf between internal
+    nodes of a multifurcating tree) rebuilds only the schedule and re-gathers the
+    leaf codes on the device; results equal a fresh engine's bit for bit, with
+    and without graph replay, in a batch where the other instances stay put."""
+    rng = np.random.default_rng(5)
+    insts = [random_instance(4, 2, 25, 400, seed=51),
+             random_instance(4, 2, 30, 333, seed=52, multifurcate=0.4),
+             random_instance(4, 2, 12, 90, seed=53)]
+    e = mp.Engine(4, 2, precision, n_instances=3)
+    for i, b in enumerate(insts):
+        e.set_tree(b.parent, b.blen, i)
+        e.set_codes(b.codes, b.leaf_nums, i)
+        e.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, i)
+    e.enable_graph(True)
+    e.logpdf_grad()
+    parents = [b.parent.copy() for b in insts]
+    for step in range(8):
+        i = step % 2
+        if i == 0:
+            parents[0] = _nni(parents[0], rng)
+        else:
+            # move a leaf of the multifurcating tree to another internal node that
+            # keeps at least two children everywhere
+            p = parents[1]
+            while True:
+                leaf = int(rng.choice(insts[1].leaf_nums))
+                old = p[leaf - 1]
+                if np.count_nonzero(p == old) < 3:
+                    continue
+                internal = [n for n in range(1, len(p) + 1) if np.any(p == n) and n != old]
+                q = p.copy()
+                q[leaf - 1] = int(rng.choice(internal))
+                parents[1] = q
+                break
+        e.set_tree(parents[i], insts[i].blen, i)
+        ll, g = e.logpdf_grad()
+        f = mp.Engine(4, 2, precision, n_instances=3)
+        for k, b in enumerate(insts):
+            f.set_tree(parents[k], b.blen, k)
+            f.set_codes(b.codes, b.leaf_nums, k)
+            f.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, k)
+        llf, gf = f.logpdf_grad()
+        f.close()
+        assert np.array_equal(ll, llf) and np.array_equal(g, gf)
+        b = insts[i]
+        bi = simulate.Instance(T.from_parent(parents[i], b.blen), parents[i], b.blen,
+                               b.leaf_nums, b.codes, b.U, b.D, b.Uinv, b.mu, b.pi, b.rates)
+        llo, go = oracle(bi)
+        rtol = F64_RTOL if precision == "f64" else F32_LL_RTOL
+        assert abs(ll[i] - llo) <= rtol * abs(llo)
+    # a topology whose leaves are not the data's leaves (a cherry's two leaves
+    # moved under leaf L: L turns internal, the cherry's node turns leaf) is refused
+    p = parents[2]
+    leaves = set(int(v) for v in insts[2].leaf_nums)
+    L = int(insts[2].leaf_nums[0])
+    cherry = next(x for x in range(1, len(p) + 1)
+                  if set(int(c) for c in np.flatnonzero(p == x) + 1) <= leaves - {L}
+                  and np.count_nonzero(p == x) == 2)
+    bad = p.copy()
+    for c in np.flatnonzero(p == cherry):
+        bad[c] = L
+    e.set_tree(bad, insts[2].blen, 2)
+    with pytest.raises(mp.MCPhyError):
+        e.logpdf_grad()
+    e.close()
+
+
 def test_batched_uneven_instances(built_lib):
     batch = simulate.hky_batch(seed=8, n=6, taxa=(5, 120), sites=(1, 3000), scale=1.0)
     for precision in ("f64", "f32"):
