@@ -95,3 +95,19 @@ def test_fp32_chain(built_lib):
         ref = lf(s.parent, s.blen)
         assert post64.logf(s.parent, s.blen) == pytest.approx(ref, rel=1e-12)
         assert post.logf(s.parent, s.blen) == pytest.approx(ref, rel=1e-6)
+
+
+def test_engine_shards_sum_to_whole(built_lib):
+    """Site shards on separate engines add up to the whole alignment (what the
+    all-reduce of a site-sharded evaluation relies on)."""
+    from mcphylo_gb300 import shard
+    inst = restriction_small(seed=14, S=1001, taxa=20)
+    model = (inst.U, inst.D, inst.Uinv, inst.mu)
+    whole, lfg, _ = shard.engine_shard(inst.parent, inst.blen, inst.codes, inst.leaf_nums, model,
+                                       inst.pi, inst.rates, 0, 1, precision="f64")
+    ll, g = lfg(inst.parent, inst.blen)
+    parts = [shard.engine_shard(inst.parent, inst.blen, inst.codes, inst.leaf_nums, model,
+                                inst.pi, inst.rates, r, 3, precision="f64") for r in range(3)]
+    res = [p[1](inst.parent, inst.blen) for p in parts]
+    assert sum(r[0] for r in res) == pytest.approx(ll, rel=1e-13)
+    np.testing.assert_allclose(sum(r[1] for r in res), g, rtol=1e-11, atol=1e-11 * np.abs(g).max())
