@@ -151,6 +151,13 @@ int mcphy_logpdf_device(mcphy_handle h, double* d_ll);
 int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_packed, double* d_ll,
                               double* d_grad_packed);
 
+/* ------------------------------------------------------------------ diagnostics
+ * One 128 x n x kd TF32 tensor-core product D = A B^T (A: 128 x kd, B: n x kd,
+ * row-major host arrays; D: 128 x n) through the operand tiles, descriptors and
+ * TMEM path of the dense-state kernels, for checking a device against a host
+ * product.  kd in {8, 16, .., 64}, n in {16, 32, 64}.  No reference counterpart. */
+int mcphy_tc_selftest(int64_t kd, int64_t n, const float* a, const float* b, float* d);
+
 /* ------------------------------------------------------------------ control
  * Stream: run on the caller's stream (a cudaStream_t cast to void*); NULL restores
  * the handle's own stream. */

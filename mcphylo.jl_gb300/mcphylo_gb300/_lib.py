@@ -53,6 +53,8 @@ SIGNATURES = {
     "mcphy_logpdf_device": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_logpdf_grad_noalloc": (c_int, [handle_t, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "mcphy_tc_selftest": (c_int, [ctypes.c_int64, ctypes.c_int64, P(ctypes.c_float),
+                                  P(ctypes.c_float), P(ctypes.c_float)]),
     "mcphy_set_stream": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_synchronize": (c_int, [handle_t]),
     "mcphy_set_tiles": (c_int, [handle_t, c_int, c_int]),
