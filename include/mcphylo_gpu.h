@@ -53,7 +53,10 @@ typedef enum {
     MCPHY_PREC_F32 = 0,       /* FP32 partials, power-of-two per-node per-site scaling,
                                  FP64 P(t) build and FP64 accumulation of scale factors
                                  and site log-likelihoods                                */
-    MCPHY_PREC_F64 = 1        /* plain FP64 path                                         */
+    MCPHY_PREC_F64 = 1,       /* plain FP64 path                                         */
+    MCPHY_PREC_TF32 = 2       /* K >= 9 only: node updates as TF32 tensor-core products
+                                 (tcgen05, FP32 accumulation), the rest as MCPHY_PREC_F32;
+                                 state-code leaves only                                  */
 } mcphy_precision;
 
 /* ------------------------------------------------------------------ single tree

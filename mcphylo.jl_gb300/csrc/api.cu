@@ -98,6 +98,12 @@ size_t real_size(const mcphy_engine* h) { return h->prec == MCPHY_PREC_F64 ? 8 :
 
 // Chooses the fused kernel's launch shape.
 void choose_tiles(mcphy_engine* h) {
+    if (h->prec == MCPHY_PREC_TF32) {
+        // one CTA of 128 threads per 128-site work item (4 x 32 sites)
+        h->spt = 4;
+        h->tpb = TC_M;
+        return;
+    }
     int spt = h->spt_req;
     if (spt == 0) spt = 1;
     if (h->prec == MCPHY_PREC_F64) spt = (h->Kp <= 4) ? std::min(spt, 2) : 1;
@@ -136,7 +142,8 @@ int layout(mcphy_engine* h) {
     h->units = 0;
     h->any_dense = false;
 
-    const int64_t rbytes = rec_bytes(Kp, int(real_size(h)));
+    const bool tc = h->prec == MCPHY_PREC_TF32;
+    const int64_t rbytes = tc ? int64_t(tc_rec_bytes(K)) : rec_bytes(Kp, int(real_size(h)));
     int64_t sched_off = 0, rec_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
             pgrad_off = 0, blen_off = 0, nsteps = 0;
     const int64_t psize = param_size(K, Kp, C);
@@ -159,6 +166,11 @@ int layout(mcphy_engine* h) {
                         "instance " + std::to_string(i) + ": tree has " +
                             std::to_string(sc.leaves.size()) + " leaves, data has " +
                             std::to_string(in.leaf_nums.size()));
+        if (tc && in.dense)
+            return fail(h, MCPHY_ERR_ARG,
+                        "instance " + std::to_string(i) +
+                            ": the tensor-core path takes state-code leaves (mcphy_set_codes or "
+                            "0/1 leaf data)");
         InstanceDesc& d = h->desc[i];
         d.J = sc.J;
         d.S = int32_t(in.S);
@@ -185,6 +197,7 @@ int layout(mcphy_engine* h) {
         // and, for code leaves, a leaf-major copy [row][S_pad] that the schedule-ordered
         // table is gathered from on the device (again after a topology change)
         h->lc_off[i] = lc_off;
+        d.lcode_off = lc_off;
         if (!in.dense) lc_off += int64_t(d.n_leaf) * d.S_pad;
         param_off += psize;
         const int64_t items = int64_t(C) * d.n_blocks;
@@ -265,15 +278,22 @@ int layout(mcphy_engine* h) {
 
     // persistent grid: as many resident warps as the SMs hold, never more than items
     int bps = 0;
-    cudaError_t oe = (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
-                                                  : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
+    cudaError_t oe = tc ? occupancy_prune_tc(K, &bps)
+                        : (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
+                                                      : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
     if (oe != cudaSuccess || bps < 1) bps = 1;
-    const int wpb = h->tpb / 32;
+    // scratch columns: per warp (SIMT kernels) or per 128-thread CTA (tensor cores)
+    const int wpb = tc ? 1 : h->tpb / 32;
     int64_t blocks = int64_t(bps) * h->sm_count;
     blocks = std::min<int64_t>(blocks, (h->n_items + wpb - 1) / wpb);
     blocks = std::max<int64_t>(blocks, 1);
-    h->warp_stride = int64_t(h->max_J) * h->spt * 32 * Kp;
-    h->pre_warp_stride = int64_t(h->max_pre) * h->spt * 32 * Kp;
+    if (tc) {
+        h->warp_stride = int64_t(h->max_J) * K * TC_M;
+        h->pre_warp_stride = int64_t(h->max_pre) * K * TC_M;
+    } else {
+        h->warp_stride = int64_t(h->max_J) * h->spt * 32 * Kp;
+        h->pre_warp_stride = int64_t(h->max_pre) * h->spt * 32 * Kp;
+    }
     // keep the scratch within half of the free device memory
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
@@ -489,7 +509,8 @@ int run(mcphy_engine* h, bool want_grad) {
     b.K = h->K;
     b.Kp = h->Kp;
     b.C = h->C;
-    CK(launch_build_records(f64, b, st));
+    const bool tc = h->prec == MCPHY_PREC_TF32;
+    CK(tc ? launch_build_records_tc(b, st) : launch_build_records(f64, b, st));
     if (h->timing) CK(cudaEventRecord(h->ev[1], st));
 
     CK(cudaMemsetAsync(h->d_counter.p, 0, 2 * sizeof(int32_t), st));
@@ -514,9 +535,11 @@ int run(mcphy_engine* h, bool want_grad) {
     a.want_grad = want_grad ? 1 : 0;
     a.wait_limit = h->inject ? 4096 : kWaitLimit;
     a.inject_timeout = h->inject == 1 ? 1 : 0;
+    a.lcodes = h->d_leafcodes.p;
     h->inject = 0;
-    CK(f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
-           : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
+    CK(tc    ? launch_prune_tc(h->K, h->blocks, a, st)
+       : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
+             : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
     if (h->timing) CK(cudaEventRecord(h->ev[2], st));
 
     ReduceArgs r{};
@@ -675,7 +698,10 @@ int mcphy_batch_create(int64_t nbase, int64_t nrates, int64_t n_instances, int p
     if (nbase < 2 || nbase > 32) return MCPHY_ERR_ARG;
     if (nrates < 1 || nrates > 64) return MCPHY_ERR_ARG;
     if (n_instances < 1 || n_instances > 65535) return MCPHY_ERR_ARG;
-    if (precision != MCPHY_PREC_F32 && precision != MCPHY_PREC_F64) return MCPHY_ERR_ARG;
+    if (precision != MCPHY_PREC_F32 && precision != MCPHY_PREC_F64 && precision != MCPHY_PREC_TF32)
+        return MCPHY_ERR_ARG;
+    // the tensor-core node updates are for dense state spaces (K >= 9)
+    if (precision == MCPHY_PREC_TF32 && nbase < 9) return MCPHY_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -1005,6 +1031,16 @@ int mcphy_enable_graph(mcphy_handle h, int on) {
 
 int mcphy_autotune(mcphy_handle h, int* out2) {
     if (!h) return MCPHY_ERR_ARG;
+    if (h->prec == MCPHY_PREC_TF32) {
+        // one launch shape: 128 sites per CTA
+        int rc = prepare(h);
+        if (rc) return rc;
+        if (out2) {
+            out2[0] = h->spt;
+            out2[1] = h->tpb;
+        }
+        return MCPHY_OK;
+    }
     std::vector<std::pair<int, int>> cand;
     if (h->prec == MCPHY_PREC_F64)
         cand = h->Kp <= 4 ? std::vector<std::pair<int, int>>{{1, 128}, {2, 128}, {1, 64}, {2, 64}}

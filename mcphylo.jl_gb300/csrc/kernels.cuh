@@ -104,7 +104,38 @@ struct PruneArgs {
     int32_t want_grad;
     int32_t wait_limit;       // iterations of every bounded mbarrier wait
     int32_t inject_timeout;   // test hook: never issue the first staging copy
+    const void* lcodes;       // leaf-major state codes [row][S_pad] (tensor-core path)
 };
+
+// ---------------------------------------------------------------- tensor-core records
+// Dense-state path (K = 9..32, kernels_tc.cu): a work item is 128 sites of one rate
+// category (one site per thread, one MMA row per site); node updates are
+// 128 x 32 x KD TF32 tcgen05 products.  Record of step j, rate r (bytes):
+//   [0, 64)  int32 hdr[16] = {op0, op1, bpush, bpop, gr0, gr1, 0...}
+//   forward part, child c = 0, 1:  P tile | PT table | row sums
+//   backward part, child c = 0, 1: dP tile | P^T tile | dPT table | dP row sums
+// "tile": a 32 x KD operand tile (tc.cuh layout, TF32-rounded, zero padded) with
+// row a, column b = M[a][b], so that D = L * tile^T is the Down vector L P^T;
+// the P^T tile holds P[b][a] at (a, b) (pre-order: pt P).  "table": K rows of
+// K4 = K rounded up to 4 FP32 entries, row s = column s of the matrix (the Down
+// vector of a leaf in state s); row sums: K4 entries (a leaf with every state).
+constexpr int TC_M = 128;
+constexpr int TC_N = 32;
+constexpr int TC_HDR = 64;
+__host__ __device__ constexpr int tc_kd(int K) { return (K + 7) / 8 * 8; }
+__host__ __device__ constexpr int tc_k4(int K) { return (K + 3) / 4 * 4; }
+__host__ __device__ constexpr int tc_tile(int K) { return TC_N * tc_kd(K) * 4; }
+__host__ __device__ constexpr int tc_tab(int K) { return K * tc_k4(K) * 4; }
+__host__ __device__ constexpr int tc_rs(int K) { return tc_k4(K) * 4; }
+__host__ __device__ constexpr int tc_fchild(int K) { return tc_tile(K) + tc_tab(K) + tc_rs(K); }
+__host__ __device__ constexpr int tc_bchild(int K) { return 2 * tc_tile(K) + tc_tab(K) + tc_rs(K); }
+__host__ __device__ constexpr int tc_fwd_bytes(int K) { return TC_HDR + 2 * tc_fchild(K); }
+__host__ __device__ constexpr int tc_rec_bytes(int K) { return tc_fwd_bytes(K) + 2 * tc_bchild(K); }
+// shared memory of one tensor-core CTA: two A tiles, two record buffers, barriers
+__host__ __device__ constexpr int tc_rec_slot(int K) { return (tc_rec_bytes(K) + 127) / 128 * 128; }
+__host__ __device__ constexpr int tc_smem_bytes(int K) {
+    return 2 * TC_M * tc_kd(K) * 4 + 2 * tc_rec_slot(K) + 256;
+}
 
 struct BuildRecArgs {
     const InstanceDesc* inst;
@@ -877,5 +908,10 @@ struct GatherArgs {
     int64_t row_words;        // S_pad x code bytes / 4
 };
 cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st);
+
+// Tensor-core path (kernels_tc.cu).
+cudaError_t launch_build_records_tc(const BuildRecArgs& a, cudaStream_t st);
+cudaError_t launch_prune_tc(int K, int blocks, const PruneArgs& a, cudaStream_t st);
+cudaError_t occupancy_prune_tc(int K, int* blocks_per_sm);
 
 }  // namespace mcphy

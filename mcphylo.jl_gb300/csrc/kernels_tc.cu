@@ -1,0 +1,599 @@
+// Dense-state (K = 9..32) likelihood + branch gradient on the fifth-generation
+// tensor cores.
+//
+// A CTA of 128 threads owns 128 sites of one rate category of one instance (thread
+// t = site t = MMA row t = TMEM lane t) and walks the whole tree for them, as the
+// SIMT kernel's warps do.  Each internal child's node update is one
+// 128 x 32 x KD TF32 tcgen05 MMA: A = the 128 sites' partials (written to shared
+// memory by the threads, TF32-rounded), B = the branch's transition tile from the
+// step record (TMA bulk copy), D in TMEM, read back with tcgen05.ld.  A leaf
+// child's Down vector is a row of the record's table picked by the state code.
+//   post-order (FelsensteinFunction logL, LikelihoodCalculator_Node.jl:82-114):
+//     D_c = L_c P_c^T (MMA for internal c), L = D_0 * D_1, power-of-two rescale,
+//     written to the CTA's global column [step][state][128 sites];
+//   pre-order (gradient, LikelihoodCalculator_Node.jl:3-78):
+//     round 1: D_c = L_c P_c^T and dD_c = L_c dP_c^T (MMAs for internal c);
+//     pt_c = pb * D_sibling, gradient term (pt_c . dD_c) / (pt_c . D_c);
+//     round 2: pb_c = pt_c P_c (MMA for internal c), rescaled; child 1's stays in
+//     registers (it is the next step), child 0's goes to the CTA's stack column.
+// Every wait is bounded: a timeout sets the error flag, the CTA drains its copies
+// and MMAs (bounded) and frees its TMEM before it returns.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "kernels.cuh"
+#include "tc.cuh"
+
+namespace mcphy {
+
+namespace {
+
+constexpr double LN2 = 0.6931471805599453094;
+constexpr uint32_t kTmemCols = 128;   // D0 | dD0 | D1 | dD1, 32 columns each
+
+// ---------------------------------------------------------------- records
+// One thread per (step, child, rate): P and dP of the child's branch in FP64 from
+// the eigensystem (the same arithmetic as build_records_kernel), written as
+// operand tiles (TF32), lookup tables and row sums; identity for a virtual branch.
+__global__ void build_records_tc_kernel(const BuildRecArgs a) {
+    const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int K = a.K, C = a.C;
+    if (tid >= int64_t(a.n_steps) * 2 * C) return;
+    const int r = int(tid % C);
+    const int c = int((tid / C) % 2);
+    const int2 sj = a.steps[tid / (2 * C)];
+    const InstanceDesc& d = a.inst[sj.x];
+    const int j = sj.y;
+    const SchedNode sn = a.sched[d.sched_off + j];
+    const int KD = tc_kd(K), K4 = tc_k4(K);
+    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(tc_rec_bytes(K));
+    if (c == 0) {
+        int* hd = reinterpret_cast<int*>(rec);
+        hd[0] = sn.op[0];
+        hd[1] = sn.op[1];
+        hd[2] = sn.bpush;
+        hd[3] = sn.bpop;
+        hd[4] = sn.br[0] < d.n_branch ? sn.br[0] : -1;
+        hd[5] = sn.br[1] < d.n_branch ? sn.br[1] : -1;
+        for (int q = 6; q < TC_HDR / 4; ++q) hd[q] = 0;
+    }
+    unsigned char* f = rec + TC_HDR + c * tc_fchild(K);
+    unsigned char* bk = rec + tc_fwd_bytes(K) + c * tc_bchild(K);
+    float* Pt = reinterpret_cast<float*>(f);
+    float* PTab = reinterpret_cast<float*>(f + tc_tile(K));
+    float* rs = reinterpret_cast<float*>(f + tc_tile(K) + tc_tab(K));
+    float* dPt = reinterpret_cast<float*>(bk);
+    float* PTt = reinterpret_cast<float*>(bk + tc_tile(K));
+    float* dPTab = reinterpret_cast<float*>(bk + 2 * tc_tile(K));
+    float* drs = reinterpret_cast<float*>(bk + 2 * tc_tile(K) + tc_tab(K));
+    // zero padding everywhere first
+    for (int e = 0; e < tc_fchild(K) / 4; ++e) reinterpret_cast<float*>(f)[e] = 0.f;
+    for (int e = 0; e < tc_bchild(K) / 4; ++e) reinterpret_cast<float*>(bk)[e] = 0.f;
+    auto put = [&](int row, int col, float p, float dp) {
+        // M[row][col] = P[row][col]: tiles at (row, col), P^T tile at (col, row),
+        // tables: row col of the table is column col of the matrix
+        *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(Pt) + tc::tile_off(row, col, KD)) =
+            tc::to_tf32(p);
+        *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dPt) + tc::tile_off(row, col, KD)) =
+            tc::to_tf32(dp);
+        *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(PTt) + tc::tile_off(col, row, KD)) =
+            tc::to_tf32(p);
+        PTab[col * K4 + row] = p;
+        dPTab[col * K4 + row] = dp;
+    };
+    const int b = sn.br[c];
+    if (b >= d.n_branch) {
+        for (int s = 0; s < K; ++s) {
+            put(s, s, 1.f, 0.f);
+            rs[s] = 1.f;
+        }
+        return;
+    }
+    const double* U = a.params + d.param_off;
+    const double* Dv = U + K * K;
+    const double* Uinv = Dv + K;
+    const double mu = Uinv[K * K];
+    const double rate = Uinv[K * K + 1 + r];
+    const double t = a.blen[d.blen_off + b];
+    double e[32], de[32];
+    for (int m = 0; m < K; ++m) {
+        const double x = exp(mu * t * Dv[m] * rate);
+        e[m] = x;
+        de[m] = Dv[m] * rate * mu * x;
+    }
+    for (int s = 0; s < K; ++s) {
+        double row = 0.0, drow = 0.0;
+        for (int k = 0; k < K; ++k) {
+            double p = 0.0, dp = 0.0;
+            for (int m = 0; m < K; ++m) {
+                p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+            }
+            row += p;
+            drow += dp;
+            put(s, k, float(p), float(dp));
+        }
+        rs[s] = float(row);
+        drs[s] = float(drow);
+    }
+}
+
+// ---------------------------------------------------------------- device helpers
+template <int KD>
+__device__ __forceinline__ void zero(float (&v)[KD]) {
+#pragma unroll
+    for (int k = 0; k < KD; ++k) v[k] = 0.f;
+}
+
+// Down vector of a leaf from a record table (K rows of K4) and its row sums.
+template <int KD>
+__device__ __forceinline__ void leaf_down(uint32_t code, uint32_t allmask, const float* tab,
+                                          const float* rs, int K, int K4, float (&out)[KD]) {
+    zero(out);
+    if (code == allmask) {
+#pragma unroll
+        for (int k = 0; k < KD; ++k)
+            if (k < K) out[k] = rs[k];
+    } else if (code != 0u && (code & (code - 1u)) == 0u) {
+        const float* row = tab + (__ffs(int(code)) - 1) * K4;
+#pragma unroll
+        for (int k = 0; k < KD; ++k)
+            if (k < K) out[k] = row[k];
+    } else {
+        uint32_t m = code;
+        while (m) {
+            const float* row = tab + (__ffs(int(m)) - 1) * K4;
+            m &= m - 1u;
+#pragma unroll
+            for (int k = 0; k < KD; ++k)
+                if (k < K) out[k] += row[k];
+        }
+    }
+}
+
+// This thread's row of an A tile (TF32-rounded).
+template <int KD>
+__device__ __forceinline__ void write_a(unsigned char* tile, int row, const float (&v)[KD]) {
+#pragma unroll
+    for (int k = 0; k < KD; k += 4)
+        *reinterpret_cast<float4*>(tile + tc::tile_off(row, k, KD)) =
+            make_float4(tc::to_tf32(v[k]), tc::to_tf32(v[k + 1]), tc::to_tf32(v[k + 2]),
+                        tc::to_tf32(v[k + 3]));
+}
+
+// KD columns of this thread's TMEM lane from column `taddr` (loads and the wait in
+// one statement, so no register is read before the load has landed).
+template <int KD>
+__device__ __forceinline__ void tmem_row(uint32_t taddr, float (&v)[KD]) {
+    tc::tmem_row_wait<KD>(taddr, v);
+}
+
+// Partial of this thread's site in a [slot][K][128] column.
+template <int KD>
+__device__ __forceinline__ void col_load(const float* col, int slot, int K, int t, float (&v)[KD]) {
+    const float* p = col + int64_t(slot) * K * TC_M + t;
+#pragma unroll
+    for (int k = 0; k < KD; ++k) v[k] = (k < K) ? p[k * TC_M] : 0.f;
+}
+template <int KD>
+__device__ __forceinline__ void col_store(float* col, int slot, int K, int t, const float (&v)[KD]) {
+    float* p = col + int64_t(slot) * K * TC_M + t;
+#pragma unroll
+    for (int k = 0; k < KD; ++k)
+        if (k < K) p[k * TC_M] = v[k];
+}
+
+// ---------------------------------------------------------------- fused sweep
+template <int KD>
+__global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const int K = a.K, K4 = tc_k4(a.K), C = a.C;
+    const int RB = tc_rec_bytes(K), FB = tc_fwd_bytes(K);
+    unsigned char* Abuf0 = sm;
+    unsigned char* Abuf1 = sm + TC_M * KD * 4;
+    unsigned char* Rbuf0 = sm + 2 * TC_M * KD * 4;
+    unsigned char* Rbuf1 = Rbuf0 + tc_rec_slot(K);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(Rbuf1 + tc_rec_slot(K));   // rec0, rec1, mma
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
+    int* item_sh = reinterpret_cast<int*>(tslot + 1);
+    float* red = reinterpret_cast<float*>(item_sh + 3);            // [2][4 warps][2]
+    double* lred = reinterpret_cast<double*>(red + 16);             // [4 warps]
+    const int t = threadIdx.x;
+    const int warp = t >> 5, lane = t & 31;
+    const uint32_t allmask = (K >= 32) ? 0xffffffffu : ((1u << K) - 1u);
+    const int limit = a.wait_limit;
+
+    if (t == 0) {
+        mbar_init(bars + 0, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init(bars + 2, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, kTmemCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *tslot;
+    const uint32_t tl = tbase + (uint32_t(warp * 32) << 16);     // this warp's lane quarter
+    const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
+    const uint32_t sbo = uint32_t(tc::tile_sbo(KD));
+    float* post = reinterpret_cast<float*>(a.post) + int64_t(blockIdx.x) * a.warp_stride;
+    float* pre = reinterpret_cast<float*>(a.pre) + int64_t(blockIdx.x) * a.pre_warp_stride;
+
+    // phases and in-flight work (thread 0 issues every copy and MMA)
+    uint32_t ph_rec = 0u;           // bit b: parity expected next on record buffer b
+    uint32_t ph_mma = 0u;
+    bool pend[2] = {false, false};
+    bool mma_pend = false;
+    bool skip_first = a.inject_timeout != 0;
+    bool failed = false;
+
+    auto rbuf = [&](int b) { return b ? Rbuf1 : Rbuf0; };
+    auto issue = [&](int b, const unsigned char* src, int bytes) {   // thread 0
+        if (skip_first) {          // test hook: this copy is never issued
+            skip_first = false;
+            return;
+        }
+        bulk_load(rbuf(b), src, uint32_t(bytes), bars + b);
+        pend[b] = true;
+    };
+    auto wait_rec = [&](int b) -> bool {
+        const bool ok = mbar_wait(bars + b, (ph_rec >> b) & 1u, limit);
+        if (ok) {
+            ph_rec ^= 1u << b;
+            pend[b] = false;
+        }
+        return ok;
+    };
+    // MMAs of one round: D (cols dcol[i]) = A tile (a_tile[i]) x B tile (b_tile[i])^T
+    auto mma_round = [&](int n, unsigned char* const* at, const unsigned char* const* bt,
+                         const uint32_t* dcol) -> bool {
+        fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (t == 0) {
+            for (int i = 0; i < n; ++i) {
+                const uint32_t a0 = tc::smem_addr(at[i]), b0 = tc::smem_addr(bt[i]);
+#pragma unroll
+                for (int s = 0; s < KD / 8; ++s)
+                    tc::mma_tf32(tbase + dcol[i], tc::smem_desc(a0 + 256u * s, tc::kCoreBytes, sbo),
+                                 tc::smem_desc(b0 + 256u * s, tc::kCoreBytes, sbo), idesc,
+                                 s > 0 ? 1u : 0u);
+            }
+            tc::mma_commit(bars + 2);
+            mma_pend = true;
+        }
+        const bool ok = mbar_wait(bars + 2, ph_mma, limit);
+        // one verdict for the whole CTA: the rounds that follow contain barriers
+        const bool bad = __syncthreads_or(!ok);
+        if (!bad) {
+            ph_mma ^= 1u;
+            if (t == 0) mma_pend = false;
+        }
+        tc::fence_after_sync();
+        return !bad;
+    };
+
+    for (;;) {
+        if (t == 0) *item_sh = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int qi = *item_sh;
+        if (qi >= a.n_items) break;
+        const int item = __ldg(a.queue + qi);
+        const int2 it = __ldg(a.items + item);
+        const InstanceDesc d = a.inst[it.x];
+        const int r = it.y / d.n_blocks;
+        const int blk = it.y - r * d.n_blocks;
+        const int site = blk * TC_M + t;
+        const bool valid = site < d.S;
+        const int J = d.J;
+        const unsigned char* recs = a.recs + d.rec_off + size_t(r) * size_t(J) * size_t(RB);
+        const uint32_t* lc = reinterpret_cast<const uint32_t*>(a.lcodes) + d.lcode_off + site;
+        const double* pi_d = a.params + d.param_off + 2 * K * K + K + 1 + C;
+        auto code_of = [&](int op) { return __ldg(lc + int64_t(-op - 1) * d.S_pad); };
+
+        // ------------------------------------------------ post-order sweep (logL)
+        if (t == 0) {
+            issue(0, recs, FB);
+            if (J > 1) issue(1, recs + RB, FB);
+        }
+        if (__syncthreads_or(!wait_rec(0))) {
+            failed = true;
+            break;
+        }
+        uint32_t eacc = 0u;
+        double ll = 0.0;
+        float Lp[KD];
+        zero(Lp);
+        for (int j = 0; j < J; ++j) {
+            const int b = j & 1;
+            const unsigned char* R = rbuf(b);
+            const int op0 = reinterpret_cast<const int*>(R)[0];
+            const int op1 = reinterpret_cast<const int*>(R)[1];
+            const unsigned char* f0 = R + TC_HDR;
+            const unsigned char* f1 = f0 + tc_fchild(K);
+            float D0[KD], D1[KD];
+            if (op0 < 0)
+                leaf_down<KD>(code_of(op0), allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
+            else {
+                float L[KD];
+                col_load<KD>(post, op0, K, t, L);
+                write_a<KD>(Abuf0, t, L);
+            }
+            if (op1 < 0)
+                leaf_down<KD>(code_of(op1), allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
+            else
+                write_a<KD>(Abuf1, t, Lp);          // op1 == j - 1: the carried partial
+            bool ok = true;
+            if (op0 >= 0 || op1 >= 0) {
+                unsigned char* at[2];
+                const unsigned char* bt[2];
+                uint32_t dc[2];
+                int n = 0;
+                if (op0 >= 0) { at[n] = Abuf0; bt[n] = f0; dc[n] = 0; ++n; }
+                if (op1 >= 0) { at[n] = Abuf1; bt[n] = f1; dc[n] = 64; ++n; }
+                ok = mma_round(n, at, bt, dc);
+                if (ok) {
+                    if (op0 >= 0) tmem_row<KD>(tl + 0, D0);
+                    if (op1 >= 0) tmem_row<KD>(tl + 64, D1);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < KD; ++k) D0[k] *= D1[k];
+            eacc += rescale<KD, float>(D0);
+            if (j + 1 < J) {
+                // later steps read operand-0 partials back from the column (both sweeps)
+                col_store<KD>(post, j, K, t, D0);
+#pragma unroll
+                for (int k = 0; k < KD; ++k) Lp[k] = D0[k];
+            } else {
+                float lik = 0.f;
+#pragma unroll
+                for (int k = 0; k < KD; ++k)
+                    if (k < K) lik = fmaf(float(__ldg(pi_d + k)), D0[k], lik);
+                const int ex = int(eacc) - J * 127;
+                ll += valid ? log(double(lik)) + double(ex) * LN2 : 0.0;
+            }
+            // end of step: the next record must be in, this buffer is free again
+            tc::fence_before_sync();
+            if (ok && j + 1 < J) ok = wait_rec(b ^ 1);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            tc::fence_after_sync();
+            if (t == 0 && j + 2 < J) issue(b, recs + size_t(j + 2) * RB, FB);
+        }
+        if (failed) break;
+        {
+            const double s = warp_sum(ll);
+            if (lane == 0) lred[warp] = s;
+            __syncthreads();
+            if (t == 0) a.pll[item] = lred[0] + lred[1] + lred[2] + lred[3];
+        }
+        if (!a.want_grad) continue;
+
+        // ------------------------------------------------ pre-order sweep (gradient)
+        float* pg = reinterpret_cast<float*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
+        if (t == 0) {
+            issue(0, recs + size_t(J - 1) * RB, RB);
+            if (J > 1) issue(1, recs + size_t(J - 2) * RB, RB);
+        }
+        if (__syncthreads_or(!wait_rec(0))) {
+            failed = true;
+            break;
+        }
+        float pb[KD];
+#pragma unroll
+        for (int k = 0; k < KD; ++k) pb[k] = (k < K) ? float(__ldg(pi_d + k)) : 0.f;
+        for (int j = J - 1; j >= 0; --j) {
+            const int sidx = J - 1 - j;
+            const int b = sidx & 1;
+            const unsigned char* R = rbuf(b);
+            const int* hd = reinterpret_cast<const int*>(R);
+            const int op0 = hd[0], op1 = hd[1], bpush = hd[2], bpop = hd[3];
+            const int gr0 = hd[4], gr1 = hd[5];
+            const unsigned char* f0 = R + TC_HDR;
+            const unsigned char* f1 = f0 + tc_fchild(K);
+            const unsigned char* k0 = R + FB;
+            const unsigned char* k1 = k0 + tc_bchild(K);
+            if (j < J - 1 && bpop >= 0) col_load<KD>(pre, bpop, K, t, pb);
+            float D0[KD], D1[KD], dD0[KD], dD1[KD];
+            if (op0 < 0) {
+                const uint32_t code = code_of(op0);
+                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
+                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K)),
+                              reinterpret_cast<const float*>(k0 + 2 * tc_tile(K) + tc_tab(K)), K, K4,
+                              dD0);
+            } else {
+                float L[KD];
+                col_load<KD>(post, op0, K, t, L);
+                write_a<KD>(Abuf0, t, L);
+            }
+            if (op1 < 0) {
+                const uint32_t code = code_of(op1);
+                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
+                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K)),
+                              reinterpret_cast<const float*>(k1 + 2 * tc_tile(K) + tc_tab(K)), K, K4,
+                              dD1);
+            } else {
+                float L[KD];
+                col_load<KD>(post, op1, K, t, L);
+                write_a<KD>(Abuf1, t, L);
+            }
+            bool ok = true;
+            const bool any = op0 >= 0 || op1 >= 0;
+            if (any) {
+                unsigned char* at[4];
+                const unsigned char* bt[4];
+                uint32_t dc[4];
+                int n = 0;
+                if (op0 >= 0) {
+                    at[n] = Abuf0; bt[n] = f0; dc[n] = 0; ++n;
+                    at[n] = Abuf0; bt[n] = k0; dc[n] = 32; ++n;
+                }
+                if (op1 >= 0) {
+                    at[n] = Abuf1; bt[n] = f1; dc[n] = 64; ++n;
+                    at[n] = Abuf1; bt[n] = k1; dc[n] = 96; ++n;
+                }
+                ok = mma_round(n, at, bt, dc);
+                if (ok) {
+                    if (op0 >= 0) {
+                        tmem_row<KD>(tl + 0, D0);
+                        tmem_row<KD>(tl + 32, dD0);
+                    }
+                    if (op1 >= 0) {
+                        tmem_row<KD>(tl + 64, D1);
+                        tmem_row<KD>(tl + 96, dD1);
+                    }
+                }
+            }
+            // child 1 first: pt_1 = pb * D_0 (D_0 is still needed for child 0's ratio)
+            float g1 = 0.f, g0 = 0.f;
+            {
+                float pt[KD];
+                float num = 0.f, den = 0.f;
+#pragma unroll
+                for (int k = 0; k < KD; ++k) {
+                    pt[k] = pb[k] * D0[k];
+                    num = fmaf(pt[k], dD1[k], num);
+                    den = fmaf(pt[k], D1[k], den);
+                }
+                g1 = valid ? __fdividef(num, den) : 0.f;
+                if (op1 >= 0) write_a<KD>(Abuf1, t, pt);
+            }
+            {
+                float pt[KD];
+                float num = 0.f, den = 0.f;
+#pragma unroll
+                for (int k = 0; k < KD; ++k) {
+                    pt[k] = pb[k] * D1[k];
+                    num = fmaf(pt[k], dD0[k], num);
+                    den = fmaf(pt[k], D0[k], den);
+                }
+                g0 = valid ? __fdividef(num, den) : 0.f;
+                if (op0 >= 0) write_a<KD>(Abuf0, t, pt);
+            }
+            g0 = warp_sum(g0);
+            g1 = warp_sum(g1);
+            if (lane == 0) {
+                red[(b * 4 + warp) * 2 + 0] = g0;
+                red[(b * 4 + warp) * 2 + 1] = g1;
+            }
+            if (ok && any) {
+                unsigned char* at[2];
+                const unsigned char* bt[2];
+                uint32_t dc[2];
+                int n = 0;
+                if (op0 >= 0) { at[n] = Abuf0; bt[n] = k0 + tc_tile(K); dc[n] = 0; ++n; }
+                if (op1 >= 0) { at[n] = Abuf1; bt[n] = k1 + tc_tile(K); dc[n] = 64; ++n; }
+                ok = mma_round(n, at, bt, dc);
+                if (ok) {
+                    float P0[KD], P1[KD];
+                    if (op0 >= 0) tmem_row<KD>(tl + 0, P0);
+                    if (op1 >= 0) tmem_row<KD>(tl + 64, P1);
+                    if (op0 >= 0) {
+                        rescale<KD, float>(P0);
+                        col_store<KD>(pre, bpush, K, t, P0);
+                    }
+                    if (op1 >= 0) {
+                        rescale<KD, float>(P1);
+#pragma unroll
+                        for (int k = 0; k < KD; ++k) pb[k] = P1[k];   // step j - 1
+                    }
+                }
+            }
+            // end of step
+            tc::fence_before_sync();
+            if (ok && j > 0) ok = wait_rec(b ^ 1);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            tc::fence_after_sync();
+            if (t == 0) {
+                if (gr0 >= 0) pg[gr0] = red[(b * 4 + 0) * 2] + red[(b * 4 + 1) * 2] +
+                                        red[(b * 4 + 2) * 2] + red[(b * 4 + 3) * 2];
+                if (gr1 >= 0) pg[gr1] = red[(b * 4 + 0) * 2 + 1] + red[(b * 4 + 1) * 2 + 1] +
+                                        red[(b * 4 + 2) * 2 + 1] + red[(b * 4 + 3) * 2 + 1];
+                if (j - 2 >= 0) issue(b, recs + size_t(j - 2) * RB, RB);
+            }
+        }
+        if (failed) break;
+    }
+    if (failed) {
+        // a bounded wait gave up: report, let this CTA's copies and MMAs land
+        // (bounded as well), then free TMEM below
+        if (t == 0) {
+            atomicExch(a.counter + 1, 1);
+            for (int b = 0; b < 2; ++b)
+                if (pend[b]) mbar_wait(bars + b, (ph_rec >> b) & 1u, limit);
+            if (mma_pend) mbar_wait(bars + 2, ph_mma, limit);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
+}
+
+template <int KD>
+cudaError_t go_tc(int blocks, const PruneArgs& a, cudaStream_t st) {
+    const int smem = tc_smem_bytes(a.K);
+    static int configured = 0;
+    if (smem > configured) {
+        cudaError_t e =
+            cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    prune_tc_kernel<KD><<<blocks, TC_M, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int KD>
+cudaError_t occ_tc(int K, int* bps) {
+    const int smem = tc_smem_bytes(K);
+    cudaError_t e =
+        cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_tc_kernel<KD>, TC_M, smem);
+    // TMEM: 512 columns per SM
+    if (e == cudaSuccess) *bps = std::min(*bps, int(512 / kTmemCols));
+    return e;
+}
+
+}  // namespace
+
+cudaError_t launch_build_records_tc(const BuildRecArgs& a, cudaStream_t st) {
+    const int64_t total = int64_t(a.n_steps) * 2 * a.C;
+    if (total == 0) return cudaSuccess;
+    const int tpb = 64;
+    build_records_tc_kernel<<<unsigned((total + tpb - 1) / tpb), tpb, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prune_tc(int K, int blocks, const PruneArgs& a, cudaStream_t st) {
+    switch (tc_kd(K)) {
+        case 16: return go_tc<16>(blocks, a, st);
+        case 24: return go_tc<24>(blocks, a, st);
+        case 32: return go_tc<32>(blocks, a, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t occupancy_prune_tc(int K, int* bps) {
+    switch (tc_kd(K)) {
+        case 16: return occ_tc<16>(K, bps);
+        case 24: return occ_tc<24>(K, bps);
+        case 32: return occ_tc<32>(K, bps);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace mcphy

@@ -56,6 +56,7 @@ struct alignas(16) InstanceDesc {
     int64_t pgrad_off;   // into the per-item gradient partials (Real units)
     int64_t blen_off;    // into the packed branch-length vector
     int64_t grad_off;    // into the packed gradient output
+    int64_t lcode_off;   // into the leaf-major code copy [row][S_pad] (code units)
 };
 
 // FP64 model parameters of one instance, packed at param_off:

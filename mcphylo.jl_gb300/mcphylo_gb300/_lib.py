@@ -18,6 +18,7 @@ ERR_ARG, ERR_SHAPE, ERR_TREE, ERR_OOM, ERR_CUDA, ERR_STATE, ERR_TIMEOUT, ERR_NO_
     -1, -2, -3, -4, -5, -6, -7, -8, -9)
 PREC_F32 = 0
 PREC_F64 = 1
+PREC_TF32 = 2
 
 i64 = ctypes.c_int64
 c_int = ctypes.c_int

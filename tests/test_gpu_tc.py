@@ -51,3 +51,120 @@ def test_random_tf32_accuracy(built_lib):
     np.testing.assert_allclose(d, want, rtol=2e-3)
     exact = a.astype(np.float64) @ b.astype(np.float64).T
     assert np.max(np.abs(d - exact) / exact) < 2e-3
+
+
+# ---------------------------------------------------------------- the TF32 likelihood path
+from gpu_cases import caterpillar, oracle, random_instance  # noqa: E402
+
+# TF32 keeps 10 mantissa bits of each operand: per-node relative error ~1e-4 that
+# partly cancels over sites.  Stated tolerances of the tensor-core path against
+# the FP64 oracle: total logL 1e-4 relative, gradient 2e-2 of max|g| norm-wise.
+TF32_LL_RTOL = 1e-4
+TF32_G_RTOL = 2e-2
+
+
+def _tf32_engine(inst):
+    import mcphylo_gb300 as mp
+    e = mp.Engine(inst.K, len(inst.rates), "tf32")
+    e.set_tree(inst.parent, inst.blen)
+    e.set_codes(inst.codes, inst.leaf_nums)
+    e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    return e
+
+
+def _check(inst, e=None):
+    llo, go = oracle(inst)
+    e = e or _tf32_engine(inst)
+    ll, g = e.logpdf_grad()
+    rel = abs(ll - llo) / abs(llo)
+    gerr = np.max(np.abs(g - go)) / np.max(np.abs(go))
+    print(f"K={inst.K} N={inst.N} S={inst.S}: logL rel {rel:.2e}, grad {gerr:.2e}")
+    assert rel <= TF32_LL_RTOL, (ll, llo)
+    assert gerr <= TF32_G_RTOL
+    assert e.logpdf() == pytest.approx(ll, rel=1e-12)
+    return ll, g
+
+
+@pytest.mark.parametrize("K,C,taxa,S,mf", [(20, 4, 24, 300, 0.0), (20, 1, 40, 128, 0.3),
+                                         (9, 2, 17, 77, 0.0), (12, 3, 30, 257, 0.2),
+                                         (32, 2, 12, 140, 0.0), (25, 1, 9, 33, 0.0)])
+def test_tf32_vs_oracle(built_lib, K, C, taxa, S, mf):
+    inst = random_instance(K, C, taxa, S, seed=K * 7 + taxa, multifurcate=mf)
+    _check(inst)
+
+
+def test_tf32_deep_caterpillar(built_lib):
+    rng = np.random.default_rng(3)
+    inst = random_instance(20, 2, 0, 200, seed=3, tree=caterpillar(60, rng))
+    _check(inst)
+
+
+def test_tf32_partially_ambiguous_codes(built_lib):
+    inst = random_instance(20, 2, 20, 150, seed=9)
+    rng = np.random.default_rng(4)
+    codes = inst.codes.copy()
+    mask = rng.random(codes.shape) < 0.1
+    codes[mask] |= np.uint32(1) << rng.integers(0, 20, size=mask.sum()).astype(np.uint32)
+    inst.codes = codes
+    _check(inst)
+
+
+def test_tf32_topology_change_and_graph(built_lib):
+    from mcphylo_gb300 import simulate, tree as T
+    inst = random_instance(20, 4, 30, 300, seed=12)
+    e = _tf32_engine(inst)
+    e.enable_graph(True)
+    _check(inst, e)
+    ll_a, g_a = e.logpdf_grad()
+    ll_b, g_b = e.logpdf_grad()
+    assert ll_a == ll_b and np.array_equal(g_a, g_b)
+    # an NNI on the live engine
+    p = inst.parent.copy()
+    rng = np.random.default_rng(2)
+    while True:
+        t = int(rng.integers(1, len(p)))
+        kids = np.flatnonzero(p == t) + 1
+        sibs = [s for s in np.flatnonzero(p == p[t - 1]) + 1 if s != t]
+        if len(kids) and p[t - 1] and sibs:
+            c, s = int(kids[0]), int(sibs[0])
+            p[c - 1], p[s - 1] = p[t - 1], t
+            break
+    e.set_tree(p, inst.blen)
+    inst2 = simulate.Instance(T.from_parent(p, inst.blen), p, inst.blen, inst.leaf_nums,
+                              inst.codes, inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    _check(inst2, e)
+
+
+def test_tf32_timeout_is_reported(built_lib):
+    import mcphylo_gb300 as mp
+    inst = random_instance(20, 2, 20, 200, seed=5)
+    e = _tf32_engine(inst)
+    ll0, g0 = e.logpdf_grad()
+    e.debug_inject(1)
+    with pytest.raises(mp.MCPhyError) as ei:
+        e.logpdf_grad()
+    assert ei.value.status == -7
+    ll1, g1 = e.logpdf_grad()
+    assert ll1 == ll0 and np.array_equal(g1, g0)
+
+
+def test_tf32_batched(built_lib):
+    import mcphylo_gb300 as mp
+    insts = [random_instance(20, 4, t, s, seed=60 + t) for t, s in ((8, 50), (35, 400), (17, 129))]
+    e = mp.Engine(20, 4, "tf32", n_instances=3)
+    for i, b in enumerate(insts):
+        e.set_tree(b.parent, b.blen, i)
+        e.set_codes(b.codes, b.leaf_nums, i)
+        e.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, i)
+    ll, g = e.logpdf_grad()
+    off = e.grad_offsets()
+    for i, b in enumerate(insts):
+        llo, go = oracle(b)
+        assert abs(ll[i] - llo) <= TF32_LL_RTOL * abs(llo)
+        assert np.max(np.abs(g[off[i]:off[i + 1]] - go)) <= TF32_G_RTOL * np.max(np.abs(go))
+
+
+def test_tf32_rejects_small_state_spaces(built_lib):
+    import mcphylo_gb300 as mp
+    with pytest.raises(Exception):
+        mp.Engine(4, 4, "tf32")
