@@ -288,7 +288,8 @@ int layout(mcphy_engine* h) {
     blocks = std::min<int64_t>(blocks, (h->n_items + wpb - 1) / wpb);
     blocks = std::max<int64_t>(blocks, 1);
     if (tc) {
-        h->warp_stride = int64_t(h->max_J) * K * TC_M;
+        // post: [step][A tile of 128 x KD floats]; pre: [slot][K][128]
+        h->warp_stride = int64_t(h->max_J) * tc_kd(K) * TC_M;
         h->pre_warp_stride = int64_t(h->max_pre) * K * TC_M;
     } else {
         h->warp_stride = int64_t(h->max_J) * h->spt * 32 * Kp;
@@ -536,6 +537,7 @@ int run(mcphy_engine* h, bool want_grad) {
     a.wait_limit = h->inject ? 4096 : kWaitLimit;
     a.inject_timeout = h->inject == 1 ? 1 : 0;
     a.lcodes = h->d_leafcodes.p;
+    a.sched = static_cast<const SchedNode*>(h->d_sched.p);
     h->inject = 0;
     CK(tc    ? launch_prune_tc(h->K, h->blocks, a, st)
        : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)

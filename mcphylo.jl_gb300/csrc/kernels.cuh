@@ -105,13 +105,16 @@ struct PruneArgs {
     int32_t wait_limit;       // iterations of every bounded mbarrier wait
     int32_t inject_timeout;   // test hook: never issue the first staging copy
     const void* lcodes;       // leaf-major state codes [row][S_pad] (tensor-core path)
+    const SchedNode* sched;   // schedule nodes (tensor-core path: sweep prologues)
 };
 
 // ---------------------------------------------------------------- tensor-core records
 // Dense-state path (K = 9..32, kernels_tc.cu): a work item is 128 sites of one rate
 // category (one site per thread, one MMA row per site); node updates are
 // 128 x 32 x KD TF32 tcgen05 products.  Record of step j, rate r (bytes):
-//   [0, 64)  int32 hdr[16] = {op0, op1, bpush, bpop, gr0, gr1, 0...}
+//   [0, 64)  int32 hdr[16] = {op0, op1, bpush, bpop, gr0, gr1, then the lookahead
+//            op0(j+1), op1(j+1), op0(j+2), op0(j-1), op1(j-1), bpop(j-1), op0(j-2),
+//            op1(j-2), 0, 0}
 //   forward part, child c = 0, 1:  P tile | PT table | row sums
 //   backward part, child c = 0, 1: dP tile | P^T tile | dPT table | dP row sums
 // "tile": a 32 x KD operand tile (tc.cuh layout, TF32-rounded, zero padded) with
@@ -131,10 +134,11 @@ __host__ __device__ constexpr int tc_fchild(int K) { return tc_tile(K) + tc_tab(
 __host__ __device__ constexpr int tc_bchild(int K) { return 2 * tc_tile(K) + tc_tab(K) + tc_rs(K); }
 __host__ __device__ constexpr int tc_fwd_bytes(int K) { return TC_HDR + 2 * tc_fchild(K); }
 __host__ __device__ constexpr int tc_rec_bytes(int K) { return tc_fwd_bytes(K) + 2 * tc_bchild(K); }
-// shared memory of one tensor-core CTA: two A tiles, two record buffers, barriers
+// shared memory of one tensor-core CTA: two stages of (two A tiles, one record
+// buffer), barriers
 __host__ __device__ constexpr int tc_rec_slot(int K) { return (tc_rec_bytes(K) + 127) / 128 * 128; }
 __host__ __device__ constexpr int tc_smem_bytes(int K) {
-    return 2 * TC_M * tc_kd(K) * 4 + 2 * tc_rec_slot(K) + 256;
+    return 4 * TC_M * tc_kd(K) * 4 + 2 * tc_rec_slot(K) + 256;
 }
 
 struct BuildRecArgs {

@@ -31,6 +31,19 @@ namespace {
 
 constexpr double LN2 = 0.6931471805599453094;
 constexpr uint32_t kTmemCols = 128;   // D0 | dD0 | D1 | dD1, 32 columns each
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+__device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes) : "memory");
+}
+// bulk copy global -> shared completing on `bar` (the expected bytes are set once)
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
 
 // ---------------------------------------------------------------- records
 // One thread per (step, child, rate): P and dP of the child's branch in FP64 from
@@ -56,7 +69,19 @@ __global__ void build_records_tc_kernel(const BuildRecArgs a) {
         hd[3] = sn.bpop;
         hd[4] = sn.br[0] < d.n_branch ? sn.br[0] : -1;
         hd[5] = sn.br[1] < d.n_branch ? sn.br[1] : -1;
-        for (int q = 6; q < TC_HDR / 4; ++q) hd[q] = 0;
+        // lookahead: operands of steps j+1, j+2 (post-order) and j-1, j-2 (pre-order),
+        // and the stack slot step j-1 pops; -1 past either end
+        const SchedNode* sc = a.sched + d.sched_off;
+        hd[6] = j + 1 < d.J ? sc[j + 1].op[0] : -1;
+        hd[7] = j + 1 < d.J ? sc[j + 1].op[1] : -1;
+        hd[8] = j + 2 < d.J ? sc[j + 2].op[0] : -1;
+        hd[9] = j >= 1 ? sc[j - 1].op[0] : -1;
+        hd[10] = j >= 1 ? sc[j - 1].op[1] : -1;
+        hd[11] = j >= 1 ? sc[j - 1].bpop : -1;
+        hd[12] = j >= 2 ? sc[j - 2].op[0] : -1;
+        hd[13] = j >= 2 ? sc[j - 2].op[1] : -1;
+        hd[14] = 0;
+        hd[15] = 0;
     }
     unsigned char* f = rec + TC_HDR + c * tc_fchild(K);
     unsigned char* bk = rec + tc_fwd_bytes(K) + c * tc_bchild(K);
@@ -185,16 +210,22 @@ __device__ __forceinline__ void col_store(float* col, int slot, int K, int t, co
 }
 
 // ---------------------------------------------------------------- fused sweep
+// Per-CTA global scratch:
+//   post: [step][A tile of 128 x KD] -- post-order partials, TF32-rounded, already in
+//         the MMA operand layout, so a later step brings one in with one bulk copy;
+//   pre:  [slot][state][128 sites] FP32 -- pre-order partials of stack slots.
+// Stage s (two, alternating by step): the step's record (forward: its first part)
+// and the A tiles of its internal children, on one mbarrier, issued two steps
+// ahead from the lookahead fields of the step record headers.
 template <int KD>
 __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
+    constexpr int TILE = TC_M * KD * 4;           // bytes of one A tile
     extern __shared__ __align__(1024) unsigned char sm[];
     const int K = a.K, K4 = tc_k4(a.K), C = a.C;
     const int RB = tc_rec_bytes(K), FB = tc_fwd_bytes(K);
-    unsigned char* Abuf0 = sm;
-    unsigned char* Abuf1 = sm + TC_M * KD * 4;
-    unsigned char* Rbuf0 = sm + 2 * TC_M * KD * 4;
-    unsigned char* Rbuf1 = Rbuf0 + tc_rec_slot(K);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(Rbuf1 + tc_rec_slot(K));   // rec0, rec1, mma
+    unsigned char* T = sm;                                       // [stage][child] A tiles
+    unsigned char* Rb = sm + 4 * TILE;                            // [stage] records
+    uint64_t* bars = reinterpret_cast<uint64_t*>(Rb + 2 * tc_rec_slot(K));   // st0, st1, mma
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
     int* item_sh = reinterpret_cast<int*>(tslot + 1);
     float* red = reinterpret_cast<float*>(item_sh + 3);            // [2][4 warps][2]
@@ -218,36 +249,45 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
     const uint32_t tl = tbase + (uint32_t(warp * 32) << 16);     // this warp's lane quarter
     const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
     const uint32_t sbo = uint32_t(tc::tile_sbo(KD));
-    float* post = reinterpret_cast<float*>(a.post) + int64_t(blockIdx.x) * a.warp_stride;
+    unsigned char* post = reinterpret_cast<unsigned char*>(a.post) +
+                          size_t(blockIdx.x) * size_t(a.warp_stride) * 4;
     float* pre = reinterpret_cast<float*>(a.pre) + int64_t(blockIdx.x) * a.pre_warp_stride;
 
-    // phases and in-flight work (thread 0 issues every copy and MMA)
-    uint32_t ph_rec = 0u;           // bit b: parity expected next on record buffer b
+    uint32_t ph_st = 0u;            // bit s: parity expected next on stage s
     uint32_t ph_mma = 0u;
-    bool pend[2] = {false, false};
-    bool mma_pend = false;
+    bool pend[2] = {false, false};  // thread 0: stage copies in flight
+    bool mma_pend = false;          // thread 0: MMAs in flight
     bool skip_first = a.inject_timeout != 0;
     bool failed = false;
 
-    auto rbuf = [&](int b) { return b ? Rbuf1 : Rbuf0; };
-    auto issue = [&](int b, const unsigned char* src, int bytes) {   // thread 0
-        if (skip_first) {          // test hook: this copy is never issued
+    auto tile = [&](int st, int c) { return T + (2 * st + c) * TILE; };
+    auto rec = [&](int st) { return Rb + st * tc_rec_slot(K); };
+    // thread 0: one step's copies on stage st -- its record (rec_bytes of it) and the
+    // post-order tiles of its internal children (op < 0: a leaf, nothing to copy)
+    auto issue = [&](int st, const unsigned char* src, int rec_bytes, int op0, int op1) {
+        if (skip_first) {           // test hook: this stage is never issued
             skip_first = false;
             return;
         }
-        bulk_load(rbuf(b), src, uint32_t(bytes), bars + b);
-        pend[b] = true;
+        const uint32_t bytes = uint32_t(rec_bytes + (op0 >= 0 ? TILE : 0) + (op1 >= 0 ? TILE : 0));
+        expect_tx(bars + st, bytes);
+        bulk_copy(rec(st), src, uint32_t(rec_bytes), bars + st);
+        if (op0 >= 0) bulk_copy(tile(st, 0), post + size_t(op0) * TILE, TILE, bars + st);
+        if (op1 >= 0) bulk_copy(tile(st, 1), post + size_t(op1) * TILE, TILE, bars + st);
+        pend[st] = true;
     };
-    auto wait_rec = [&](int b) -> bool {
-        const bool ok = mbar_wait(bars + b, (ph_rec >> b) & 1u, limit);
+    auto wait_stage = [&](int st) -> bool {
+        const bool ok = mbar_wait(bars + st, (ph_st >> st) & 1u, limit);
         if (ok) {
-            ph_rec ^= 1u << b;
-            pend[b] = false;
+            ph_st ^= 1u << st;
+            pend[st] = false;
         }
         return ok;
     };
-    // MMAs of one round: D (cols dcol[i]) = A tile (a_tile[i]) x B tile (b_tile[i])^T
-    auto mma_round = [&](int n, unsigned char* const* at, const unsigned char* const* bt,
+    // one round of MMAs: D (TMEM column dcol[i]) = A tile at[i] x B tile bt[i]^T.
+    // Returns this warp's verdict (uniform in the warp); the CTA's verdict is taken
+    // at the end of the step.
+    auto mma_round = [&](int n, const unsigned char* const* at, const unsigned char* const* bt,
                          const uint32_t* dcol) -> bool {
         fence_proxy_async();
         tc::fence_before_sync();
@@ -265,15 +305,13 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             tc::mma_commit(bars + 2);
             mma_pend = true;
         }
-        const bool ok = mbar_wait(bars + 2, ph_mma, limit);
-        // one verdict for the whole CTA: the rounds that follow contain barriers
-        const bool bad = __syncthreads_or(!ok);
-        if (!bad) {
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(bars + 2, ph_mma, limit));
+        if (ok) {
             ph_mma ^= 1u;
             if (t == 0) mma_pend = false;
         }
         tc::fence_after_sync();
-        return !bad;
+        return ok;
     };
 
     for (;;) {
@@ -292,14 +330,16 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         const unsigned char* recs = a.recs + d.rec_off + size_t(r) * size_t(J) * size_t(RB);
         const uint32_t* lc = reinterpret_cast<const uint32_t*>(a.lcodes) + d.lcode_off + site;
         const double* pi_d = a.params + d.param_off + 2 * K * K + K + 1 + C;
-        auto code_of = [&](int op) { return __ldg(lc + int64_t(-op - 1) * d.S_pad); };
+        const SchedNode* sc = a.sched + d.sched_off;
+        auto code_of = [&](int op) { return op < 0 ? __ldg(lc + int64_t(-op - 1) * d.S_pad) : 0u; };
 
         // ------------------------------------------------ post-order sweep (logL)
         if (t == 0) {
-            issue(0, recs, FB);
-            if (J > 1) issue(1, recs + RB, FB);
+            issue(0, recs, FB, sc[0].op[0], -1);
+            if (J > 1) issue(1, recs + RB, FB, sc[1].op[0], -1);
         }
-        if (__syncthreads_or(!wait_rec(0))) {
+        uint32_t code0 = code_of(sc[0].op[0]), code1 = code_of(sc[0].op[1]);
+        if (__syncthreads_or(!wait_stage(0))) {
             failed = true;
             break;
         }
@@ -309,45 +349,43 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         zero(Lp);
         for (int j = 0; j < J; ++j) {
             const int b = j & 1;
-            const unsigned char* R = rbuf(b);
-            const int op0 = reinterpret_cast<const int*>(R)[0];
-            const int op1 = reinterpret_cast<const int*>(R)[1];
+            const unsigned char* R = rec(b);
+            const int* hd = reinterpret_cast<const int*>(R);
+            const int op0 = hd[0], op1 = hd[1];
             const unsigned char* f0 = R + TC_HDR;
             const unsigned char* f1 = f0 + tc_fchild(K);
+            // leaf codes of the next step, one step ahead
+            const uint32_t ncode0 = (j + 1 < J) ? code_of(hd[6]) : 0u;
+            const uint32_t ncode1 = (j + 1 < J) ? code_of(hd[7]) : 0u;
+            if (op1 >= 0) write_a<KD>(tile(b, 1), t, Lp);   // op1 == j - 1: the carried partial
             float D0[KD], D1[KD];
-            if (op0 < 0)
-                leaf_down<KD>(code_of(op0), allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
-            else {
-                float L[KD];
-                col_load<KD>(post, op0, K, t, L);
-                write_a<KD>(Abuf0, t, L);
-            }
-            if (op1 < 0)
-                leaf_down<KD>(code_of(op1), allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
-            else
-                write_a<KD>(Abuf1, t, Lp);          // op1 == j - 1: the carried partial
             bool ok = true;
             if (op0 >= 0 || op1 >= 0) {
-                unsigned char* at[2];
+                const unsigned char* at[2];
                 const unsigned char* bt[2];
                 uint32_t dc[2];
                 int n = 0;
-                if (op0 >= 0) { at[n] = Abuf0; bt[n] = f0; dc[n] = 0; ++n; }
-                if (op1 >= 0) { at[n] = Abuf1; bt[n] = f1; dc[n] = 64; ++n; }
+                if (op0 >= 0) { at[n] = tile(b, 0); bt[n] = f0; dc[n] = 0; ++n; }
+                if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = f1; dc[n] = 64; ++n; }
                 ok = mma_round(n, at, bt, dc);
                 if (ok) {
                     if (op0 >= 0) tmem_row<KD>(tl + 0, D0);
                     if (op1 >= 0) tmem_row<KD>(tl + 64, D1);
                 }
             }
+            if (op0 < 0)
+                leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
+            if (op1 < 0)
+                leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
 #pragma unroll
             for (int k = 0; k < KD; ++k) D0[k] *= D1[k];
             eacc += rescale<KD, float>(D0);
             if (j + 1 < J) {
-                // later steps read operand-0 partials back from the column (both sweeps)
-                col_store<KD>(post, j, K, t, D0);
+                // TF32 copy in operand layout for the steps that read it back
+                write_a<KD>(post + size_t(j) * TILE, t, D0);
+                fence_proxy_async_global();
 #pragma unroll
                 for (int k = 0; k < KD; ++k) Lp[k] = D0[k];
             } else {
@@ -358,15 +396,18 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 const int ex = int(eacc) - J * 127;
                 ll += valid ? log(double(lik)) + double(ex) * LN2 : 0.0;
             }
-            // end of step: the next record must be in, this buffer is free again
+            code0 = ncode0;
+            code1 = ncode1;
+            // end of step: the next stage must be in; this stage is free again
+            const int f2op0 = hd[8];
             tc::fence_before_sync();
-            if (ok && j + 1 < J) ok = wait_rec(b ^ 1);
+            if (ok && j + 1 < J) ok = wait_stage(b ^ 1);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
             }
             tc::fence_after_sync();
-            if (t == 0 && j + 2 < J) issue(b, recs + size_t(j + 2) * RB, FB);
+            if (t == 0 && j + 2 < J) issue(b, recs + size_t(j + 2) * RB, FB, f2op0, -1);
         }
         if (failed) break;
         {
@@ -380,10 +421,12 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         // ------------------------------------------------ pre-order sweep (gradient)
         float* pg = reinterpret_cast<float*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
         if (t == 0) {
-            issue(0, recs + size_t(J - 1) * RB, RB);
-            if (J > 1) issue(1, recs + size_t(J - 2) * RB, RB);
+            issue(0, recs + size_t(J - 1) * RB, RB, sc[J - 1].op[0], sc[J - 1].op[1]);
+            if (J > 1) issue(1, recs + size_t(J - 2) * RB, RB, sc[J - 2].op[0], sc[J - 2].op[1]);
         }
-        if (__syncthreads_or(!wait_rec(0))) {
+        code0 = code_of(sc[J - 1].op[0]);
+        code1 = code_of(sc[J - 1].op[1]);
+        if (__syncthreads_or(!wait_stage(0))) {
             failed = true;
             break;
         }
@@ -391,94 +434,94 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
 #pragma unroll
         for (int k = 0; k < KD; ++k) pb[k] = (k < K) ? float(__ldg(pi_d + k)) : 0.f;
         for (int j = J - 1; j >= 0; --j) {
-            const int sidx = J - 1 - j;
-            const int b = sidx & 1;
-            const unsigned char* R = rbuf(b);
+            const int b = (J - 1 - j) & 1;
+            const unsigned char* R = rec(b);
             const int* hd = reinterpret_cast<const int*>(R);
-            const int op0 = hd[0], op1 = hd[1], bpush = hd[2], bpop = hd[3];
+            const int op0 = hd[0], op1 = hd[1], bpush = hd[2];
             const int gr0 = hd[4], gr1 = hd[5];
             const unsigned char* f0 = R + TC_HDR;
             const unsigned char* f1 = f0 + tc_fchild(K);
             const unsigned char* k0 = R + FB;
             const unsigned char* k1 = k0 + tc_bchild(K);
-            if (j < J - 1 && bpop >= 0) col_load<KD>(pre, bpop, K, t, pb);
-            float D0[KD], D1[KD], dD0[KD], dD1[KD];
-            if (op0 < 0) {
-                const uint32_t code = code_of(op0);
-                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
-                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K)),
-                              reinterpret_cast<const float*>(k0 + 2 * tc_tile(K) + tc_tab(K)), K, K4,
-                              dD0);
-            } else {
-                float L[KD];
-                col_load<KD>(post, op0, K, t, L);
-                write_a<KD>(Abuf0, t, L);
-            }
-            if (op1 < 0) {
-                const uint32_t code = code_of(op1);
-                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
-                leaf_down<KD>(code, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K)),
-                              reinterpret_cast<const float*>(k1 + 2 * tc_tile(K) + tc_tab(K)), K, K4,
-                              dD1);
-            } else {
-                float L[KD];
-                col_load<KD>(post, op1, K, t, L);
-                write_a<KD>(Abuf1, t, L);
+            // next step's leaf codes and stacked pre-order partial, one step ahead
+            uint32_t ncode0 = 0u, ncode1 = 0u;
+            float pbn[KD];
+            zero(pbn);
+            if (j > 0) {
+                ncode0 = code_of(hd[9]);
+                ncode1 = code_of(hd[10]);
+                if (hd[11] >= 0) col_load<KD>(pre, hd[11], K, t, pbn);
             }
             bool ok = true;
             const bool any = op0 >= 0 || op1 >= 0;
             if (any) {
-                unsigned char* at[4];
+                const unsigned char* at[4];
                 const unsigned char* bt[4];
                 uint32_t dc[4];
                 int n = 0;
                 if (op0 >= 0) {
-                    at[n] = Abuf0; bt[n] = f0; dc[n] = 0; ++n;
-                    at[n] = Abuf0; bt[n] = k0; dc[n] = 32; ++n;
+                    at[n] = tile(b, 0); bt[n] = f0; dc[n] = 0; ++n;
+                    at[n] = tile(b, 0); bt[n] = k0; dc[n] = 32; ++n;
                 }
                 if (op1 >= 0) {
-                    at[n] = Abuf1; bt[n] = f1; dc[n] = 64; ++n;
-                    at[n] = Abuf1; bt[n] = k1; dc[n] = 96; ++n;
+                    at[n] = tile(b, 1); bt[n] = f1; dc[n] = 64; ++n;
+                    at[n] = tile(b, 1); bt[n] = k1; dc[n] = 96; ++n;
                 }
                 ok = mma_round(n, at, bt, dc);
-                if (ok) {
-                    if (op0 >= 0) {
-                        tmem_row<KD>(tl + 0, D0);
-                        tmem_row<KD>(tl + 32, dD0);
-                    }
-                    if (op1 >= 0) {
-                        tmem_row<KD>(tl + 64, D1);
-                        tmem_row<KD>(tl + 96, dD1);
-                    }
-                }
             }
-            // child 1 first: pt_1 = pb * D_0 (D_0 is still needed for child 0's ratio)
-            float g1 = 0.f, g0 = 0.f;
+            // Down vectors of both children (TMEM for internal ones, tables for leaves)
+            float D0[KD], D1[KD];
+            if (op0 >= 0) {
+                if (ok) tmem_row<KD>(tl + 0, D0);
+            } else {
+                leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
+            }
+            if (op1 >= 0) {
+                if (ok) tmem_row<KD>(tl + 64, D1);
+            } else {
+                leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
+                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
+            }
+            // child 1: pt_1 = pb * D_0; child 0: pt_0 = pb * D_1
+            float g0, g1;
             {
-                float pt[KD];
+                float pt[KD], dD[KD];
+                if (op1 >= 0) {
+                    if (ok) tmem_row<KD>(tl + 96, dD);
+                } else {
+                    leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K)),
+                                  reinterpret_cast<const float*>(k1 + 2 * tc_tile(K) + tc_tab(K)), K,
+                                  K4, dD);
+                }
                 float num = 0.f, den = 0.f;
 #pragma unroll
                 for (int k = 0; k < KD; ++k) {
                     pt[k] = pb[k] * D0[k];
-                    num = fmaf(pt[k], dD1[k], num);
+                    num = fmaf(pt[k], dD[k], num);
                     den = fmaf(pt[k], D1[k], den);
                 }
                 g1 = valid ? __fdividef(num, den) : 0.f;
-                if (op1 >= 0) write_a<KD>(Abuf1, t, pt);
+                if (op1 >= 0) write_a<KD>(tile(b, 1), t, pt);
             }
             {
-                float pt[KD];
+                float pt[KD], dD[KD];
+                if (op0 >= 0) {
+                    if (ok) tmem_row<KD>(tl + 32, dD);
+                } else {
+                    leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K)),
+                                  reinterpret_cast<const float*>(k0 + 2 * tc_tile(K) + tc_tab(K)), K,
+                                  K4, dD);
+                }
                 float num = 0.f, den = 0.f;
 #pragma unroll
                 for (int k = 0; k < KD; ++k) {
                     pt[k] = pb[k] * D1[k];
-                    num = fmaf(pt[k], dD0[k], num);
+                    num = fmaf(pt[k], dD[k], num);
                     den = fmaf(pt[k], D0[k], den);
                 }
                 g0 = valid ? __fdividef(num, den) : 0.f;
-                if (op0 >= 0) write_a<KD>(Abuf0, t, pt);
+                if (op0 >= 0) write_a<KD>(tile(b, 0), t, pt);
             }
             g0 = warp_sum(g0);
             g1 = warp_sum(g1);
@@ -486,32 +529,36 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 red[(b * 4 + warp) * 2 + 0] = g0;
                 red[(b * 4 + warp) * 2 + 1] = g1;
             }
-            if (ok && any) {
-                unsigned char* at[2];
+            if (any) {
+                const unsigned char* at[2];
                 const unsigned char* bt[2];
                 uint32_t dc[2];
                 int n = 0;
-                if (op0 >= 0) { at[n] = Abuf0; bt[n] = k0 + tc_tile(K); dc[n] = 0; ++n; }
-                if (op1 >= 0) { at[n] = Abuf1; bt[n] = k1 + tc_tile(K); dc[n] = 64; ++n; }
-                ok = mma_round(n, at, bt, dc);
+                if (op0 >= 0) { at[n] = tile(b, 0); bt[n] = k0 + tc_tile(K); dc[n] = 0; ++n; }
+                if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = k1 + tc_tile(K); dc[n] = 64; ++n; }
+                const bool ok2 = mma_round(n, at, bt, dc);
+                ok = ok && ok2;
                 if (ok) {
-                    float P0[KD], P1[KD];
-                    if (op0 >= 0) tmem_row<KD>(tl + 0, P0);
-                    if (op1 >= 0) tmem_row<KD>(tl + 64, P1);
                     if (op0 >= 0) {
+                        float P0[KD];
+                        tmem_row<KD>(tl + 0, P0);
                         rescale<KD, float>(P0);
                         col_store<KD>(pre, bpush, K, t, P0);
                     }
                     if (op1 >= 0) {
-                        rescale<KD, float>(P1);
-#pragma unroll
-                        for (int k = 0; k < KD; ++k) pb[k] = P1[k];   // step j - 1
+                        tmem_row<KD>(tl + 64, pbn);     // step j - 1's own partial: carried
+                        rescale<KD, float>(pbn);
                     }
                 }
             }
+#pragma unroll
+            for (int k = 0; k < KD; ++k) pb[k] = pbn[k];
+            code0 = ncode0;
+            code1 = ncode1;
             // end of step
+            const int b2op0 = hd[12], b2op1 = hd[13];
             tc::fence_before_sync();
-            if (ok && j > 0) ok = wait_rec(b ^ 1);
+            if (ok && j > 0) ok = wait_stage(b ^ 1);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -522,7 +569,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                                         red[(b * 4 + 2) * 2] + red[(b * 4 + 3) * 2];
                 if (gr1 >= 0) pg[gr1] = red[(b * 4 + 0) * 2 + 1] + red[(b * 4 + 1) * 2 + 1] +
                                         red[(b * 4 + 2) * 2 + 1] + red[(b * 4 + 3) * 2 + 1];
-                if (j - 2 >= 0) issue(b, recs + size_t(j - 2) * RB, RB);
+                if (j - 2 >= 0) issue(b, recs + size_t(j - 2) * RB, RB, b2op0, b2op1);
             }
         }
         if (failed) break;
@@ -533,7 +580,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         if (t == 0) {
             atomicExch(a.counter + 1, 1);
             for (int b = 0; b < 2; ++b)
-                if (pend[b]) mbar_wait(bars + b, (ph_rec >> b) & 1u, limit);
+                if (pend[b]) mbar_wait(bars + b, (ph_st >> b) & 1u, limit);
             if (mma_pend) mbar_wait(bars + 2, ph_mma, limit);
         }
     }
@@ -550,6 +597,9 @@ cudaError_t go_tc(int blocks, const PruneArgs& a, cudaStream_t st) {
         cudaError_t e =
             cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 100);
+        if (e != cudaSuccess) return e;
         configured = smem;
     }
     prune_tc_kernel<KD><<<blocks, TC_M, smem, st>>>(a);
@@ -561,6 +611,8 @@ cudaError_t occ_tc(int K, int* bps) {
     const int smem = tc_smem_bytes(K);
     cudaError_t e =
         cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_tc_kernel<KD>, TC_M, smem);
     // TMEM: 512 columns per SM
