@@ -56,11 +56,13 @@ def test_random_tf32_accuracy(built_lib):
 # ---------------------------------------------------------------- the TF32 likelihood path
 from gpu_cases import caterpillar, oracle, random_instance  # noqa: E402
 
-# TF32 keeps 10 mantissa bits of each operand: per-node relative error ~1e-4 that
-# partly cancels over sites.  Stated tolerances of the tensor-core path against
-# the FP64 oracle: total logL 1e-4 relative, gradient 2e-2 of max|g| norm-wise.
-TF32_LL_RTOL = 1e-4
-TF32_G_RTOL = 2e-2
+# TF32 keeps 10 mantissa bits of each operand: a relative error of up to 2^-11 per
+# rounded operand and node, which accumulates with tree depth (measured: 4e-5 to
+# 1.5e-4 on total logL, the larger on a 60-deep caterpillar; gradient entries within
+# 5e-4 of max|g|).  Stated tolerances of the tensor-core path against the FP64
+# oracle: total logL 5e-4 relative, gradient 5e-3 of max|g|.
+TF32_LL_RTOL = 5e-4
+TF32_G_RTOL = 5e-3
 
 
 def _tf32_engine(inst):
