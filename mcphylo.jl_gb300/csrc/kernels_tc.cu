@@ -614,10 +614,25 @@ cudaError_t occ_tc(int K, int* bps) {
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_tc_kernel<KD>, TC_M, smem);
-    // TMEM: 512 columns per SM
-    if (e == cudaSuccess) *bps = std::min(*bps, int(512 / kTmemCols));
-    return e;
+    // resident CTAs per SM from the kernel's own limits: registers (allocated per
+    // warp in units of 256), shared memory (plus the 1 KB each CTA reserves) and
+    // TMEM (512 columns per SM)
+    cudaFuncAttributes fa{};
+    e = cudaFuncGetAttributes(&fa, prune_tc_kernel<KD>);
+    if (e != cudaSuccess) return e;
+    int dev = 0, regs_sm = 0, smem_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) !=
+        cudaSuccess)
+        return e;
+    const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
+    const int by_regs = regs_sm / (regs_warp * (TC_M / 32));
+    const int by_smem = smem_sm / (smem + 1024);
+    *bps = std::max(1, std::min({by_regs, by_smem, int(512 / kTmemCols)}));
+    return cudaSuccess;
 }
 
 }  // namespace
