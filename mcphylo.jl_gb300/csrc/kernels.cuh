@@ -220,11 +220,25 @@ template <typename Real> struct ExpBias;
 template <> struct ExpBias<float> { static constexpr int value = 127; };
 template <> struct ExpBias<double> { static constexpr int value = 1023; };
 
+// maximum of v, as a pairwise tree (short dependency chains)
+template <int KP, typename Real>
+__device__ __forceinline__ Real vmax(const Real (&v)[KP]) {
+    if constexpr (KP == 1) {
+        return v[0];
+    } else {
+        constexpr int H = KP / 2;
+        Real lo[H], hi[KP - H];
+#pragma unroll
+        for (int k = 0; k < H; ++k) lo[k] = v[k];
+#pragma unroll
+        for (int k = H; k < KP; ++k) hi[k - H] = v[k];
+        return rmax(vmax<H, Real>(lo), vmax<KP - H, Real>(hi));
+    }
+}
+
 template <int KP, typename Real>
 __device__ __forceinline__ uint32_t rescale(Real (&v)[KP]) {
-    Real m = v[0];
-#pragma unroll
-    for (int k = 1; k < KP; ++k) m = rmax(m, v[k]);
+    const Real m = vmax<KP, Real>(v);
     Real f;
     const uint32_t field = scale_bits(m, f);
 #pragma unroll

@@ -46,22 +46,26 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
 }
 
 // ---------------------------------------------------------------- records
-// One thread per (step, child, rate): P and dP of the child's branch in FP64 from
-// the eigensystem (the same arithmetic as build_records_kernel), written as
-// operand tiles (TF32), lookup tables and row sums; identity for a virtual branch.
-__global__ void build_records_tc_kernel(const BuildRecArgs a) {
+// One thread per (step, child, rate, row s < 32): row s of P and dP of the child's
+// branch in FP64 from the eigensystem (the same arithmetic as build_records_kernel),
+// written as row s of the P and dP tiles, column s of the P^T tile and of the two
+// tables, and entry s of the row sums -- zero where s or the column is a padding
+// state; identity for a virtual branch.
+__global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, C = a.C;
-    if (tid >= int64_t(a.n_steps) * 2 * C) return;
-    const int r = int(tid % C);
-    const int c = int((tid / C) % 2);
-    const int2 sj = a.steps[tid / (2 * C)];
+    if (tid >= int64_t(a.n_steps) * 2 * C * TC_N) return;
+    const int s = int(tid % TC_N);
+    const int64_t u = tid / TC_N;
+    const int r = int(u % C);
+    const int c = int((u / C) % 2);
+    const int2 sj = a.steps[u / (2 * C)];
     const InstanceDesc& d = a.inst[sj.x];
     const int j = sj.y;
     const SchedNode sn = a.sched[d.sched_off + j];
     const int KD = tc_kd(K), K4 = tc_k4(K);
     unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(tc_rec_bytes(K));
-    if (c == 0) {
+    if (c == 0 && s == 0) {
         int* hd = reinterpret_cast<int*>(rec);
         hd[0] = sn.op[0];
         hd[1] = sn.op[1];
@@ -85,63 +89,67 @@ __global__ void build_records_tc_kernel(const BuildRecArgs a) {
     }
     unsigned char* f = rec + TC_HDR + c * tc_fchild(K);
     unsigned char* bk = rec + tc_fwd_bytes(K) + c * tc_bchild(K);
-    float* Pt = reinterpret_cast<float*>(f);
+    unsigned char* Pt = f;
     float* PTab = reinterpret_cast<float*>(f + tc_tile(K));
     float* rs = reinterpret_cast<float*>(f + tc_tile(K) + tc_tab(K));
-    float* dPt = reinterpret_cast<float*>(bk);
-    float* PTt = reinterpret_cast<float*>(bk + tc_tile(K));
+    unsigned char* dPt = bk;
+    unsigned char* PTt = bk + tc_tile(K);
     float* dPTab = reinterpret_cast<float*>(bk + 2 * tc_tile(K));
     float* drs = reinterpret_cast<float*>(bk + 2 * tc_tile(K) + tc_tab(K));
-    // zero padding everywhere first
-    for (int e = 0; e < tc_fchild(K) / 4; ++e) reinterpret_cast<float*>(f)[e] = 0.f;
-    for (int e = 0; e < tc_bchild(K) / 4; ++e) reinterpret_cast<float*>(bk)[e] = 0.f;
-    auto put = [&](int row, int col, float p, float dp) {
-        // M[row][col] = P[row][col]: tiles at (row, col), P^T tile at (col, row),
-        // tables: row col of the table is column col of the matrix
-        *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(Pt) + tc::tile_off(row, col, KD)) =
-            tc::to_tf32(p);
-        *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(dPt) + tc::tile_off(row, col, KD)) =
-            tc::to_tf32(dp);
-        *reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(PTt) + tc::tile_off(col, row, KD)) =
-            tc::to_tf32(p);
-        PTab[col * K4 + row] = p;
-        dPTab[col * K4 + row] = dp;
+    auto at = [&](unsigned char* tile, int row, int col) -> float& {
+        return *reinterpret_cast<float*>(tile + tc::tile_off(row, col, KD));
     };
     const int b = sn.br[c];
-    if (b >= d.n_branch) {
-        for (int s = 0; s < K; ++s) {
-            put(s, s, 1.f, 0.f);
-            rs[s] = 1.f;
-        }
-        return;
-    }
-    const double* U = a.params + d.param_off;
-    const double* Dv = U + K * K;
-    const double* Uinv = Dv + K;
-    const double mu = Uinv[K * K];
-    const double rate = Uinv[K * K + 1 + r];
-    const double t = a.blen[d.blen_off + b];
+    const bool real = b < d.n_branch;
     double e[32], de[32];
-    for (int m = 0; m < K; ++m) {
-        const double x = exp(mu * t * Dv[m] * rate);
-        e[m] = x;
-        de[m] = Dv[m] * rate * mu * x;
+    const double* U = a.params + d.param_off;
+    const double* Uinv = U + K * K + K;
+    if (real && s < K) {
+        const double* Dv = U + K * K;
+        const double mu = Uinv[K * K];
+        const double rate = Uinv[K * K + 1 + r];
+        const double t = a.blen[d.blen_off + b];
+        for (int m = 0; m < K; ++m) {
+            const double x = exp(mu * t * Dv[m] * rate);
+            e[m] = x;
+            de[m] = Dv[m] * rate * mu * x;
+        }
     }
-    for (int s = 0; s < K; ++s) {
-        double row = 0.0, drow = 0.0;
-        for (int k = 0; k < K; ++k) {
-            double p = 0.0, dp = 0.0;
-            for (int m = 0; m < K; ++m) {
-                p += U[s + K * m] * e[m] * Uinv[m + K * k];
-                dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+    double row = 0.0, drow = 0.0;
+    float prow[32];
+    for (int k = 0; k < KD; ++k) {
+        double p = 0.0, dp = 0.0;
+        if (s < K && k < K) {
+            if (real) {
+                for (int m = 0; m < K; ++m) {
+                    p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                    dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+                }
+            } else {
+                p = (s == k) ? 1.0 : 0.0;
             }
             row += p;
             drow += dp;
-            put(s, k, float(p), float(dp));
+            PTab[k * K4 + s] = float(p);          // column s of row k of the table
+            dPTab[k * K4 + s] = float(dp);
         }
+        prow[k] = float(p);
+        at(Pt, s, k) = tc::to_tf32(float(p));
+        at(dPt, s, k) = tc::to_tf32(float(dp));
+    }
+    if (s >= K && s < K4)
+        for (int k = 0; k < K; ++k) {
+            PTab[k * K4 + s] = 0.f;
+            dPTab[k * K4 + s] = 0.f;
+        }
+    if (s < K4) {
         rs[s] = float(row);
         drs[s] = float(drow);
     }
+    // column s of the P^T tile: P^T tile (n, s) = P[s][n] -> row n < 32, column s < KD
+    if (s < KD)
+        for (int n = 0; n < TC_N; ++n)
+            at(PTt, n, s) = tc::to_tf32((n < K && s < K) ? prow[n] : 0.f);
 }
 
 // ---------------------------------------------------------------- device helpers
@@ -151,30 +159,49 @@ __device__ __forceinline__ void zero(float (&v)[KD]) {
     for (int k = 0; k < KD; ++k) v[k] = 0.f;
 }
 
-// Down vector of a leaf from a record table (K rows of K4) and its row sums.
+// Down vector of a leaf from a record table (K rows of K4, zero beyond K) and its
+// row sums (K4 entries, zero beyond K); 16-byte loads.
 template <int KD>
 __device__ __forceinline__ void leaf_down(uint32_t code, uint32_t allmask, const float* tab,
                                           const float* rs, int K, int K4, float (&out)[KD]) {
     zero(out);
-    if (code == allmask) {
+    const float* row = nullptr;
+    if (code == allmask) row = rs;
+    else if (code != 0u && (code & (code - 1u)) == 0u) row = tab + (__ffs(int(code)) - 1) * K4;
+    if (row) {
 #pragma unroll
-        for (int k = 0; k < KD; ++k)
-            if (k < K) out[k] = rs[k];
-    } else if (code != 0u && (code & (code - 1u)) == 0u) {
-        const float* row = tab + (__ffs(int(code)) - 1) * K4;
-#pragma unroll
-        for (int k = 0; k < KD; ++k)
-            if (k < K) out[k] = row[k];
-    } else {
-        uint32_t m = code;
-        while (m) {
-            const float* row = tab + (__ffs(int(m)) - 1) * K4;
-            m &= m - 1u;
-#pragma unroll
-            for (int k = 0; k < KD; ++k)
-                if (k < K) out[k] += row[k];
-        }
+        for (int k = 0; k < KD; k += 4)
+            if (k < K4) {
+                const float4 x = *reinterpret_cast<const float4*>(row + k);
+                out[k] = x.x; out[k + 1] = x.y; out[k + 2] = x.z; out[k + 3] = x.w;
+            }
+        return;
     }
+    uint32_t m = code;
+    while (m) {
+        const float* rw = tab + (__ffs(int(m)) - 1) * K4;
+        m &= m - 1u;
+#pragma unroll
+        for (int k = 0; k < KD; k += 4)
+            if (k < K4) {
+                const float4 x = *reinterpret_cast<const float4*>(rw + k);
+                out[k] += x.x; out[k + 1] += x.y; out[k + 2] += x.z; out[k + 3] += x.w;
+            }
+    }
+}
+
+// (pt . x, pt . y) with four independent partial sums each
+template <int KD>
+__device__ __forceinline__ void dot2(const float (&pt)[KD], const float (&x)[KD],
+                                     const float (&y)[KD], float& nx, float& ny) {
+    float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < KD; ++k) {
+        ax[k & 3] = fmaf(pt[k], x[k], ax[k & 3]);
+        ay[k & 3] = fmaf(pt[k], y[k], ay[k & 3]);
+    }
+    nx = (ax[0] + ax[1]) + (ax[2] + ax[3]);
+    ny = (ay[0] + ay[1]) + (ay[2] + ay[3]);
 }
 
 // This thread's row of an A tile (TF32-rounded).
@@ -494,13 +521,10 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                                   reinterpret_cast<const float*>(k1 + 2 * tc_tile(K) + tc_tab(K)), K,
                                   K4, dD);
                 }
-                float num = 0.f, den = 0.f;
 #pragma unroll
-                for (int k = 0; k < KD; ++k) {
-                    pt[k] = pb[k] * D0[k];
-                    num = fmaf(pt[k], dD[k], num);
-                    den = fmaf(pt[k], D1[k], den);
-                }
+                for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D0[k];
+                float num, den;
+                dot2<KD>(pt, dD, D1, num, den);
                 g1 = valid ? __fdividef(num, den) : 0.f;
                 if (op1 >= 0) write_a<KD>(tile(b, 1), t, pt);
             }
@@ -513,13 +537,10 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                                   reinterpret_cast<const float*>(k0 + 2 * tc_tile(K) + tc_tab(K)), K,
                                   K4, dD);
                 }
-                float num = 0.f, den = 0.f;
 #pragma unroll
-                for (int k = 0; k < KD; ++k) {
-                    pt[k] = pb[k] * D1[k];
-                    num = fmaf(pt[k], dD[k], num);
-                    den = fmaf(pt[k], D0[k], den);
-                }
+                for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D1[k];
+                float num, den;
+                dot2<KD>(pt, dD, D0, num, den);
                 g0 = valid ? __fdividef(num, den) : 0.f;
                 if (op0 >= 0) write_a<KD>(tile(b, 0), t, pt);
             }
@@ -638,9 +659,9 @@ cudaError_t occ_tc(int K, int* bps) {
 }  // namespace
 
 cudaError_t launch_build_records_tc(const BuildRecArgs& a, cudaStream_t st) {
-    const int64_t total = int64_t(a.n_steps) * 2 * a.C;
+    const int64_t total = int64_t(a.n_steps) * 2 * a.C * TC_N;
     if (total == 0) return cudaSuccess;
-    const int tpb = 64;
+    const int tpb = 128;
     build_records_tc_kernel<<<unsigned((total + tpb - 1) / tpb), tpb, 0, st>>>(a);
     return cudaGetLastError();
 }
