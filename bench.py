@@ -83,6 +83,28 @@ def make_engine(insts, precision, tiles=None):
     return e
 
 
+def tc_algorithmic_bytes(insts, grad=True):
+    """Bytes the tensor-core kernel must move per evaluation: every post-order partial
+    of an internal non-root step written once (as a TF32 operand tile, KD entries
+    per site) and read once by the gradient sweep, the leaf state codes read once
+    (4 bytes), the per-item gradient partials written once."""
+    import mcphylo_gb300 as mp
+    total = 0
+    for b in insts:
+        KD = (b.K + 7) // 8 * 8
+        info = mp.schedule_info(b.parent)
+        C = len(b.rates)
+        blocks = -(-b.S // 128)
+        lanes = blocks * 128 * C
+        total += len(b.leaf_nums) * b.S * 4
+        if grad:
+            total += 2 * lanes * (info["internal"] - 1) * KD * 4
+            total += C * blocks * (b.N - 1) * 4
+        else:
+            total += lanes * (info["internal"] - 1) * KD * 4
+    return total
+
+
 def algorithmic_bytes(insts, spt, real_bytes, grad=True):
     """Bytes the fused kernel must move per evaluation: every post-order partial of
     an internal non-root step written once and read once (gradient mode only), the
@@ -413,15 +435,18 @@ def run_gpu(args, rank, world):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
 
+    prec = args.precision
+    if prec == "tf32" and insts[0].K < 9:
+        raise SystemExit("--precision tf32 is the dense-state path (K >= 9)")
     if args.tiles == "auto":
         # the library's autotuner: times each launch shape on this problem
-        e = make_engine(insts, "f32")
+        e = make_engine(insts, prec)
         tiles = e.autotune()
         tune = {"chosen_by": "mcphy_autotune"}
     else:
         tiles = tuple(int(x) for x in args.tiles.split("x"))
         tune = {}
-        e = make_engine(insts, "f32", tiles)
+        e = make_engine(insts, prec, tiles)
     M = len(insts)
     off = e.grad_offsets()
     G = int(off[-1])
@@ -556,8 +581,33 @@ def run_gpu(args, rank, world):
                "within_1e-6": bool(rel_inst <= 1e-6)}
         e64.close()
 
+    # the SIMT FP32 path on the same inputs, beside the tensor-core one
+    simt = None
+    if prec == "tf32":
+        e32 = make_engine(insts, "f32")
+        e32.autotune()
+        e32.enable_timing(True)
+        e32.set_all_branch_lengths(host_sets[args.warmup + args.steps - 1])
+        e32.logpdf_grad() if args.mode == "grad" else e32.logpdf()
+        t32 = []
+        for _ in range(args.fp64_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e32.logpdf_grad() if args.mode == "grad" else e32.logpdf()
+            tm = e32.timing()
+            t32.append(tm["build_p_ms"] + tm["prune_ms"] + tm["reduce_ms"])
+        ms32 = statistics.mean(t32)
+        simt = {"value": units * world / (ms32 / 1e3), "ms_per_step": ms32,
+                "speedup_tensor_over_simt": ms32 / ms}
+        e32.close()
+
     real_b = 4
-    alg = algorithmic_bytes(insts, tiles[0], real_b, args.mode == "grad")
+    if prec == "tf32":
+        alg = tc_algorithmic_bytes(insts, args.mode == "grad")
+        kname = "prune_tc_kernel<%d>" % ((insts[0].K + 7) // 8 * 8)
+    else:
+        alg = algorithmic_bytes(insts, tiles[0], real_b, args.mode == "grad")
+        kname = "prune_kernel<4,float,%d>" % tiles[0]
     pr = statistics.mean(prune_ms)
     achieved = alg / (pr / 1e3) / 1e9
     # DRAM bytes of one prune launch from the committed ncu capture: bytes per unit
@@ -568,7 +618,8 @@ def run_gpu(args, rank, world):
     if os.path.exists(tpath):
         try:
             tj = json.load(open(tpath))
-            if tj.get("kernel") == "prune_kernel<4,float,%d>" % tiles[0] and insts[0].K == 4:
+            tj = tj.get(kname, tj) if isinstance(tj, dict) else tj
+            if tj.get("kernel") == kname and (prec == "tf32" or insts[0].K == 4):
                 traffic = float(tj["bytes_per_unit"]) * units
                 traffic_note = (f"ncu dram bytes of a {tj['captured_workload']} launch scaled by "
                                 f"units ({tj['bytes_per_unit']} B/unit)")
@@ -576,7 +627,7 @@ def run_gpu(args, rank, world):
             traffic = None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_note,
-                "kernel": "prune_kernel<4,float,%d>" % tiles[0],
+                "kernel": kname,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg,
                 "algorithmic_bytes_per_unit": alg / units,
@@ -594,14 +645,15 @@ def run_gpu(args, rank, world):
         "logL-only site-node updates/s, FP32-scaled vs plain FP64 GPU at ≤1e-6 rel err"
     out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32",
+           "vs_baseline": None, "dtype": "tf32" if prec == "tf32" else "f32",
            "data": "synthetic (seeded simulation down Yule trees)",
            "config": dict(cfg, tiles={"sites_per_thread": tiles[0], "threads_per_block": tiles[1]},
                           l2="flushed between steps (512 MB write, outside the timed events)",
                           parallelism="replicas" if world > 1 else "single GPU"),
            "clocks": clocks, "e2e": e2e,
            "gpu_launches": (4 if args.mode == "grad" else 4) * args.steps,
-           "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64, "fp32_error": err,
+           "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
+           "error_vs_fp64": err, "fp32_simt": simt,
            "kernel_ms": {"build_transition": statistics.mean(build_ms), "prune": pr,
                          "reduce": statistics.mean(red_ms)},
            "autotune_prune_ms": tune, "wall_s_timed_loop": wall}
@@ -628,6 +680,8 @@ def main():
     ap.add_argument("--nuts-adapt", type=int, default=200)
     ap.add_argument("--nuts-seed", type=int, default=1)
     ap.add_argument("--nuts-target", type=float, default=0.8)
+    ap.add_argument("--precision", default="f32", choices=["f32", "tf32"],
+                    help="f32: FP32-scaled SIMT path; tf32: tensor-core node updates (K >= 9)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -810,24 +810,27 @@ prune_kernel(const PruneArgs a) {
 }
 
 // ---------------------------------------------------------------- step records
-// One thread per (step record, child, rate): P(t) and dP/dt of the child's branch
-// in FP64, in the reference's order (out2[m,i] = U[m,i] * exp(mu * t * D[i] * rate);
-// P = out2 * Uinv), written transposed with the row-sum row; identity for the
-// zero-length virtual branches.  The c == 0 thread also writes the header.
+// One thread per (step record, child, rate, row s < Kp): row s of P(t) and dP/dt of
+// the child's branch in FP64, in the reference's order (out2[m,i] = U[m,i] *
+// exp(mu * t * D[i] * rate); P = out2 * Uinv), written transposed (column s of
+// P^T and dP^T) with entry s of the row-sum row; identity for the zero-length
+// virtual branches.  The (c == 0, s == 0) thread also writes the header.
 template <typename Real>
 __global__ void build_records_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, Kp = a.Kp, C = a.C;
-    if (tid >= int64_t(a.n_steps) * 2 * C) return;
-    const int r = int(tid % C);
-    const int c = int((tid / C) % 2);
-    const int2 sj = a.steps[tid / (2 * C)];
+    if (tid >= int64_t(a.n_steps) * 2 * C * Kp) return;
+    const int s = int(tid % Kp);
+    const int64_t u = tid / Kp;
+    const int r = int(u % C);
+    const int c = int((u / C) % 2);
+    const int2 sj = a.steps[u / (2 * C)];
     const InstanceDesc& d = a.inst[sj.x];
     const int j = sj.y;
     const SchedNode sn = a.sched[d.sched_off + j];
     const int bytes = rec_bytes(Kp, sizeof(Real));
     unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(bytes);
-    if (c == 0) {
+    if (c == 0 && s == 0) {
         int* hd = reinterpret_cast<int*>(rec);
         hd[0] = sn.op[0];
         hd[1] = sn.op[1];
@@ -850,14 +853,12 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     Real* dPT = PT + mat;
     const int b = sn.br[c];
     if (b >= d.n_branch) {
-        for (int s = 0; s < Kp; ++s) {
-            for (int k = 0; k < Kp; ++k) {
-                PT[k * Kp + s] = Real(k == s ? 1 : 0);
-                dPT[k * Kp + s] = Real(0);
-            }
-            PT[Kp * Kp + s] = Real(s < K ? 1 : 0);
-            dPT[Kp * Kp + s] = Real(0);
+        for (int k = 0; k < Kp; ++k) {
+            PT[k * Kp + s] = Real(k == s ? 1 : 0);
+            dPT[k * Kp + s] = Real(0);
         }
+        PT[Kp * Kp + s] = Real(s < K ? 1 : 0);
+        dPT[Kp * Kp + s] = Real(0);
         return;
     }
     const double* U = a.params + d.param_off;
@@ -867,31 +868,30 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const double rate = Uinv[K * K + 1 + r];
     const double t = a.blen[d.blen_off + b];
     double e[32], de[32];
-    for (int m = 0; m < K; ++m) {
-        const double x = exp(mu * t * Dv[m] * rate);
-        e[m] = x;
-        de[m] = Dv[m] * rate * mu * x;
-    }
-    for (int s = 0; s < Kp; ++s) {
-        double rs = 0.0, drs = 0.0;
-        for (int k = 0; k < Kp; ++k) {
-            double p = 0.0, dp = 0.0;
-            if (s < K && k < K) {
-                for (int m = 0; m < K; ++m) {
-                    p += U[s + K * m] * e[m] * Uinv[m + K * k];
-                    dp += U[s + K * m] * de[m] * Uinv[m + K * k];
-                }
-                rs += p;
-                drs += dp;
-            } else {
-                p = (s == k) ? 1.0 : 0.0;
-            }
-            PT[k * Kp + s] = Real(p);
-            dPT[k * Kp + s] = Real(dp);
+    if (s < K)
+        for (int m = 0; m < K; ++m) {
+            const double x = exp(mu * t * Dv[m] * rate);
+            e[m] = x;
+            de[m] = Dv[m] * rate * mu * x;
         }
-        PT[Kp * Kp + s] = Real(rs);
-        dPT[Kp * Kp + s] = Real(drs);
+    double rs = 0.0, drs = 0.0;
+    for (int k = 0; k < Kp; ++k) {
+        double p = 0.0, dp = 0.0;
+        if (s < K && k < K) {
+            for (int m = 0; m < K; ++m) {
+                p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+            }
+            rs += p;
+            drs += dp;
+        } else {
+            p = (s == k) ? 1.0 : 0.0;
+        }
+        PT[k * Kp + s] = Real(p);
+        dPT[k * Kp + s] = Real(dp);
     }
+    PT[Kp * Kp + s] = Real(rs);
+    dPT[Kp * Kp + s] = Real(drs);
 }
 
 // ---------------------------------------------------------------- reduction
