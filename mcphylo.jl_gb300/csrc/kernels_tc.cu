@@ -30,7 +30,8 @@ namespace mcphy {
 namespace {
 
 constexpr double LN2 = 0.6931471805599453094;
-constexpr uint32_t kTmemCols = 128;   // D0 | dD0 | D1 | dD1, 32 columns each
+// TMEM columns: D0 | dD0 | D1 | dD1 | pre-order products of children 0 and 1, 32 each
+constexpr uint32_t kTmemCols = 256;
 __device__ __forceinline__ void fence_proxy_async_global() {
     asm volatile("fence.proxy.async.global;" ::: "memory");
 }
@@ -446,6 +447,9 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         if (!a.want_grad) continue;
 
         // ------------------------------------------------ pre-order sweep (gradient)
+        // Software-pipelined: one MMA round per step carries step j's pre-order
+        // products (TMEM columns 128, 160) and step j-1's Down / dDown products
+        // (columns 0, 32, 64, 96), which do not depend on step j.
         float* pg = reinterpret_cast<float*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
         if (t == 0) {
             issue(0, recs + size_t(J - 1) * RB, RB, sc[J - 1].op[0], sc[J - 1].op[1]);
@@ -456,6 +460,31 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         if (__syncthreads_or(!wait_stage(0))) {
             failed = true;
             break;
+        }
+        // round 1 of a step: D_c and dD_c of its internal children, from stage st
+        auto add_round1 = [&](int st, int& n, const unsigned char** at, const unsigned char** bt,
+                              uint32_t* dc) {
+            const unsigned char* Rs = rec(st);
+            const int* h = reinterpret_cast<const int*>(Rs);
+            const unsigned char* g0 = Rs + TC_HDR;
+            const unsigned char* q0 = Rs + FB;
+            if (h[0] >= 0) {
+                at[n] = tile(st, 0); bt[n] = g0; dc[n] = 0; ++n;
+                at[n] = tile(st, 0); bt[n] = q0; dc[n] = 32; ++n;
+            }
+            if (h[1] >= 0) {
+                at[n] = tile(st, 1); bt[n] = g0 + tc_fchild(K); dc[n] = 64; ++n;
+                at[n] = tile(st, 1); bt[n] = q0 + tc_bchild(K); dc[n] = 96; ++n;
+            }
+        };
+        bool okr;
+        {
+            const unsigned char* at[4];
+            const unsigned char* bt[4];
+            uint32_t dc[4];
+            int n = 0;
+            if (t == 0) add_round1(0, n, at, bt, dc);
+            okr = mma_round(n, at, bt, dc);
         }
         float pb[KD];
 #pragma unroll
@@ -479,33 +508,16 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 ncode1 = code_of(hd[10]);
                 if (hd[11] >= 0) col_load<KD>(pre, hd[11], K, t, pbn);
             }
-            bool ok = true;
-            const bool any = op0 >= 0 || op1 >= 0;
-            if (any) {
-                const unsigned char* at[4];
-                const unsigned char* bt[4];
-                uint32_t dc[4];
-                int n = 0;
-                if (op0 >= 0) {
-                    at[n] = tile(b, 0); bt[n] = f0; dc[n] = 0; ++n;
-                    at[n] = tile(b, 0); bt[n] = k0; dc[n] = 32; ++n;
-                }
-                if (op1 >= 0) {
-                    at[n] = tile(b, 1); bt[n] = f1; dc[n] = 64; ++n;
-                    at[n] = tile(b, 1); bt[n] = k1; dc[n] = 96; ++n;
-                }
-                ok = mma_round(n, at, bt, dc);
-            }
             // Down vectors of both children (TMEM for internal ones, tables for leaves)
             float D0[KD], D1[KD];
             if (op0 >= 0) {
-                if (ok) tmem_row<KD>(tl + 0, D0);
+                if (okr) tmem_row<KD>(tl + 0, D0);
             } else {
                 leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
                               reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
             }
             if (op1 >= 0) {
-                if (ok) tmem_row<KD>(tl + 64, D1);
+                if (okr) tmem_row<KD>(tl + 64, D1);
             } else {
                 leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
                               reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
@@ -515,7 +527,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             {
                 float pt[KD], dD[KD];
                 if (op1 >= 0) {
-                    if (ok) tmem_row<KD>(tl + 96, dD);
+                    if (okr) tmem_row<KD>(tl + 96, dD);
                 } else {
                     leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K)),
                                   reinterpret_cast<const float*>(k1 + 2 * tc_tile(K) + tc_tab(K)), K,
@@ -531,7 +543,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             {
                 float pt[KD], dD[KD];
                 if (op0 >= 0) {
-                    if (ok) tmem_row<KD>(tl + 32, dD);
+                    if (okr) tmem_row<KD>(tl + 32, dD);
                 } else {
                     leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K)),
                                   reinterpret_cast<const float*>(k0 + 2 * tc_tile(K) + tc_tab(K)), K,
@@ -550,26 +562,36 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 red[(b * 4 + warp) * 2 + 0] = g0;
                 red[(b * 4 + warp) * 2 + 1] = g1;
             }
-            if (any) {
-                const unsigned char* at[2];
-                const unsigned char* bt[2];
-                uint32_t dc[2];
+            // step j - 1's stage must be in for its round 1
+            bool ok = okr;
+            bool next_in = false;
+            if (j > 0) {
+                next_in = wait_stage(b ^ 1);
+                ok = ok && next_in;
+            }
+            {
+                const unsigned char* at[6];
+                const unsigned char* bt[6];
+                uint32_t dc[6];
                 int n = 0;
-                if (op0 >= 0) { at[n] = tile(b, 0); bt[n] = k0 + tc_tile(K); dc[n] = 0; ++n; }
-                if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = k1 + tc_tile(K); dc[n] = 64; ++n; }
-                const bool ok2 = mma_round(n, at, bt, dc);
-                ok = ok && ok2;
-                if (ok) {
-                    if (op0 >= 0) {
-                        float P0[KD];
-                        tmem_row<KD>(tl + 0, P0);
-                        rescale<KD, float>(P0);
-                        col_store<KD>(pre, bpush, K, t, P0);
-                    }
-                    if (op1 >= 0) {
-                        tmem_row<KD>(tl + 64, pbn);     // step j - 1's own partial: carried
-                        rescale<KD, float>(pbn);
-                    }
+                if (t == 0) {
+                    if (op0 >= 0) { at[n] = tile(b, 0); bt[n] = k0 + tc_tile(K); dc[n] = 128; ++n; }
+                    if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = k1 + tc_tile(K); dc[n] = 160; ++n; }
+                    if (next_in) add_round1(b ^ 1, n, at, bt, dc);
+                }
+                okr = mma_round(n, at, bt, dc);
+            }
+            ok = ok && okr;
+            if (okr) {
+                if (op0 >= 0) {
+                    float P0[KD];
+                    tmem_row<KD>(tl + 128, P0);
+                    rescale<KD, float>(P0);
+                    col_store<KD>(pre, bpush, K, t, P0);
+                }
+                if (op1 >= 0) {
+                    tmem_row<KD>(tl + 160, pbn);        // step j - 1's own partial: carried
+                    rescale<KD, float>(pbn);
                 }
             }
 #pragma unroll
@@ -579,7 +601,6 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             // end of step
             const int b2op0 = hd[12], b2op1 = hd[13];
             tc::fence_before_sync();
-            if (ok && j > 0) ok = wait_stage(b ^ 1);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
