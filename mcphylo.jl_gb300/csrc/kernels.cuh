@@ -114,7 +114,8 @@ struct PruneArgs {
 // 128 x 32 x KD TF32 tcgen05 products.  Record of step j, rate r (bytes):
 //   [0, 64)  int32 hdr[16] = {op0, op1, bpush, bpop, gr0, gr1, then the lookahead
 //            op0(j+1), op1(j+1), op0(j+2), op0(j-1), op1(j-1), bpop(j-1), op0(j-2),
-//            op1(j-2), 0, 0}
+//            op1(j-2), then fpush (>= 0: a later post-order step reads the partial
+//            back), 0}
 //   forward part, child c = 0, 1:  P tile | PT table | row sums
 //   backward part, child c = 0, 1: dP tile | P^T tile | dPT table | dP row sums
 // "tile": a 32 x KD operand tile (tc.cuh layout, TF32-rounded, zero padded) with

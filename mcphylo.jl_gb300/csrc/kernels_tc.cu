@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
         hd[11] = j >= 1 ? sc[j - 1].bpop : -1;
         hd[12] = j >= 2 ? sc[j - 2].op[0] : -1;
         hd[13] = j >= 2 ? sc[j - 2].op[1] : -1;
-        hd[14] = 0;
+        hd[14] = sn.fpush;      // >= 0: a later post-order step reads this partial back
         hd[15] = 0;
     }
     unsigned char* f = rec + TC_HDR + c * tc_fchild(K);
@@ -411,9 +411,11 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             for (int k = 0; k < KD; ++k) D0[k] *= D1[k];
             eacc += rescale<KD, float>(D0);
             if (j + 1 < J) {
-                // TF32 copy in operand layout for the steps that read it back
+                // TF32 copy in operand layout for the steps that read it back; the
+                // copies a later post-order step reads by TMA are fenced now, the
+                // rest once before the gradient sweep
                 write_a<KD>(post + size_t(j) * TILE, t, D0);
-                fence_proxy_async_global();
+                if (hd[14] >= 0) fence_proxy_async_global();
 #pragma unroll
                 for (int k = 0; k < KD; ++k) Lp[k] = D0[k];
             } else {
@@ -438,6 +440,9 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             if (t == 0 && j + 2 < J) issue(b, recs + size_t(j + 2) * RB, FB, f2op0, -1);
         }
         if (failed) break;
+        // every post-order copy is read back by TMA in the gradient sweep: fence them
+        // before the barrier that precedes its first copy
+        fence_proxy_async_global();
         {
             const double s = warp_sum(ll);
             if (lane == 0) lred[warp] = s;
