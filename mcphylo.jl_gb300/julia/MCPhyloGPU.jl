@@ -6,7 +6,7 @@ Julia binding of libmcphylo_gpu.so for MCPhylo.jl: `GPUPhyloDist` wraps a
 
     using MCPhylo, MCPhyloGPU
     pd  = PhyloDist(tree, pden, [1.0], [1.0], JC)
-    gpd = GPUPhyloDist(pd; precision = :f32)      # or :f64 (plain FP64 path)
+    gpd = GPUPhyloDist(pd; precision = :f32)      # or :f64 (plain FP64), :tf32 (K >= 9)
     logpdf(gpd, df); gradlogpdf(gpd, df)          # same results and layouts as pd
 
 In a model, use `GPUPhyloDist(PhyloDist(...))` where the reference uses
@@ -39,7 +39,7 @@ end
 function Handle(nbase::Int, nrates::Int, precision::Symbol)
     r = Ref{Ptr{Cvoid}}(C_NULL)
     st = ccall((:mcphy_create, libmcphy), Cint, (Int64, Int64, Cint, Ref{Ptr{Cvoid}}),
-               nbase, nrates, precision === :f32 ? 0 : 1, r)
+               nbase, nrates, precision === :f32 ? 0 : precision === :tf32 ? 2 : 1, r)
     check(st, C_NULL)
     h = Handle(r[])
     finalizer(h) do x
