@@ -534,6 +534,7 @@ def run_gpu(args, rank, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e_ms = 1e3 * statistics.mean(e2e_t)
     e2e = {"value": units * world / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+           "ms_per_step_min": 1e3 * min(e2e_t), "ms_per_step_median": 1e3 * statistics.median(e2e_t),
            "h2d_bytes_per_step": int(base.nbytes),
            "d2h_bytes_per_step": int((M + (G if args.mode == "grad" else 0)) * 8),
            "path": "mcphy_batch_set_all_branch_lengths + mcphy_batch_logpdf%s (host arrays), "
