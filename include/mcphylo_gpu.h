@@ -54,9 +54,10 @@ typedef enum {
                                  FP64 P(t) build and FP64 accumulation of scale factors
                                  and site log-likelihoods                                */
     MCPHY_PREC_F64 = 1,       /* plain FP64 path                                         */
-    MCPHY_PREC_TF32 = 2       /* K >= 9 only: node updates as TF32 tensor-core products
+    MCPHY_PREC_TF32 = 2,      /* K >= 9 only: node updates as TF32 tensor-core products
                                  (tcgen05, FP32 accumulation), the rest as MCPHY_PREC_F32;
                                  state-code leaves only                                  */
+    MCPHY_PREC_BF16 = 3       /* as MCPHY_PREC_TF32 with BF16 operands                   */
 } mcphy_precision;
 
 /* ------------------------------------------------------------------ single tree
@@ -155,11 +156,12 @@ int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_packed, doubl
                               double* d_grad_packed);
 
 /* ------------------------------------------------------------------ diagnostics
- * One 128 x n x kd TF32 tensor-core product D = A B^T (A: 128 x kd, B: n x kd,
- * row-major host arrays; D: 128 x n) through the operand tiles, descriptors and
- * TMEM path of the dense-state kernels, for checking a device against a host
- * product.  kd in {8, 16, .., 64}, n in {16, 32, 64}.  No reference counterpart. */
-int mcphy_tc_selftest(int64_t kd, int64_t n, const float* a, const float* b, float* d);
+ * One 128 x n x kd tensor-core product D = A B^T (A: 128 x kd, B: n x kd, row-major
+ * host arrays, used as TF32 (bf16 = 0) or BF16 (bf16 = 1); D: 128 x n, FP32) through
+ * the operand tiles, descriptors and TMEM path of the dense-state kernels, for
+ * checking a device against a host product.  kd a multiple of 8 (TF32) or 16 (BF16)
+ * in [8, 64], n in {16, 32, 64}.  No reference counterpart. */
+int mcphy_tc_selftest(int64_t kd, int64_t n, int bf16, const float* a, const float* b, float* d);
 
 /* ------------------------------------------------------------------ control
  * Stream: run on the caller's stream (a cudaStream_t cast to void*); NULL restores

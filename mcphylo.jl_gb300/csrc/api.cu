@@ -95,10 +95,14 @@ int check_instance(mcphy_engine* h, int64_t i) {
 }
 
 size_t real_size(const mcphy_engine* h) { return h->prec == MCPHY_PREC_F64 ? 8 : 4; }
+// tensor-core path: -1 none, 0 TF32 operands, 1 BF16 operands
+int tc_fmt(const mcphy_engine* h) {
+    return h->prec == MCPHY_PREC_TF32 ? 0 : h->prec == MCPHY_PREC_BF16 ? 1 : -1;
+}
 
 // Chooses the fused kernel's launch shape.
 void choose_tiles(mcphy_engine* h) {
-    if (h->prec == MCPHY_PREC_TF32) {
+    if (tc_fmt(h) >= 0) {
         // one CTA of 128 threads per 128-site work item (4 x 32 sites)
         h->spt = 4;
         h->tpb = TC_M;
@@ -142,8 +146,9 @@ int layout(mcphy_engine* h) {
     h->units = 0;
     h->any_dense = false;
 
-    const bool tc = h->prec == MCPHY_PREC_TF32;
-    const int64_t rbytes = tc ? int64_t(tc_rec_bytes(K)) : rec_bytes(Kp, int(real_size(h)));
+    const int fmt = tc_fmt(h);
+    const bool tc = fmt >= 0;
+    const int64_t rbytes = tc ? int64_t(tc_rec_bytes(K, fmt)) : rec_bytes(Kp, int(real_size(h)));
     int64_t sched_off = 0, rec_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
             pgrad_off = 0, blen_off = 0, nsteps = 0;
     const int64_t psize = param_size(K, Kp, C);
@@ -278,7 +283,7 @@ int layout(mcphy_engine* h) {
 
     // persistent grid: as many resident warps as the SMs hold, never more than items
     int bps = 0;
-    cudaError_t oe = tc ? occupancy_prune_tc(K, &bps)
+    cudaError_t oe = tc ? occupancy_prune_tc(fmt, K, &bps)
                         : (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
                                                       : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
     if (oe != cudaSuccess || bps < 1) bps = 1;
@@ -288,8 +293,8 @@ int layout(mcphy_engine* h) {
     blocks = std::min<int64_t>(blocks, (h->n_items + wpb - 1) / wpb);
     blocks = std::max<int64_t>(blocks, 1);
     if (tc) {
-        // post: [step][A tile of 128 x KD floats]; pre: [slot][K][128]
-        h->warp_stride = int64_t(h->max_J) * tc_kd(K) * TC_M;
+        // post: [step][A tile] in 4-byte units; pre: [slot][K][128] floats
+        h->warp_stride = int64_t(h->max_J) * tc_atile(K, fmt) / 4;
         h->pre_warp_stride = int64_t(h->max_pre) * K * TC_M;
     } else {
         h->warp_stride = int64_t(h->max_J) * h->spt * 32 * Kp;
@@ -510,8 +515,9 @@ int run(mcphy_engine* h, bool want_grad) {
     b.K = h->K;
     b.Kp = h->Kp;
     b.C = h->C;
-    const bool tc = h->prec == MCPHY_PREC_TF32;
-    CK(tc ? launch_build_records_tc(b, st) : launch_build_records(f64, b, st));
+    const int fmt = tc_fmt(h);
+    const bool tc = fmt >= 0;
+    CK(tc ? launch_build_records_tc(fmt, b, st) : launch_build_records(f64, b, st));
     if (h->timing) CK(cudaEventRecord(h->ev[1], st));
 
     CK(cudaMemsetAsync(h->d_counter.p, 0, 2 * sizeof(int32_t), st));
@@ -539,7 +545,7 @@ int run(mcphy_engine* h, bool want_grad) {
     a.lcodes = h->d_leafcodes.p;
     a.sched = static_cast<const SchedNode*>(h->d_sched.p);
     h->inject = 0;
-    CK(tc    ? launch_prune_tc(h->K, h->blocks, a, st)
+    CK(tc    ? launch_prune_tc(fmt, h->K, h->blocks, a, st)
        : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
              : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
     if (h->timing) CK(cudaEventRecord(h->ev[2], st));
@@ -700,10 +706,12 @@ int mcphy_batch_create(int64_t nbase, int64_t nrates, int64_t n_instances, int p
     if (nbase < 2 || nbase > 32) return MCPHY_ERR_ARG;
     if (nrates < 1 || nrates > 64) return MCPHY_ERR_ARG;
     if (n_instances < 1 || n_instances > 65535) return MCPHY_ERR_ARG;
-    if (precision != MCPHY_PREC_F32 && precision != MCPHY_PREC_F64 && precision != MCPHY_PREC_TF32)
+    if (precision != MCPHY_PREC_F32 && precision != MCPHY_PREC_F64 &&
+        precision != MCPHY_PREC_TF32 && precision != MCPHY_PREC_BF16)
         return MCPHY_ERR_ARG;
     // the tensor-core node updates are for dense state spaces (K >= 9)
-    if (precision == MCPHY_PREC_TF32 && nbase < 9) return MCPHY_ERR_ARG;
+    if ((precision == MCPHY_PREC_TF32 || precision == MCPHY_PREC_BF16) && nbase < 9)
+        return MCPHY_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -1033,7 +1041,7 @@ int mcphy_enable_graph(mcphy_handle h, int on) {
 
 int mcphy_autotune(mcphy_handle h, int* out2) {
     if (!h) return MCPHY_ERR_ARG;
-    if (h->prec == MCPHY_PREC_TF32) {
+    if (tc_fmt(h) >= 0) {
         // one launch shape: 128 sites per CTA
         int rc = prepare(h);
         if (rc) return rc;

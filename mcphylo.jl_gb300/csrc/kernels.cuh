@@ -111,14 +111,15 @@ struct PruneArgs {
 // ---------------------------------------------------------------- tensor-core records
 // Dense-state path (K = 9..32, kernels_tc.cu): a work item is 128 sites of one rate
 // category (one site per thread, one MMA row per site); node updates are
-// 128 x 32 x KD TF32 tcgen05 products.  Record of step j, rate r (bytes):
+// 128 x 32 x KD tcgen05 products, TF32 or BF16 operands with FP32 accumulation.
+// Record of step j, rate r (bytes):
 //   [0, 64)  int32 hdr[16] = {op0, op1, bpush, bpop, gr0, gr1, then the lookahead
 //            op0(j+1), op1(j+1), op0(j+2), op0(j-1), op1(j-1), bpop(j-1), op0(j-2),
 //            op1(j-2), then fpush (>= 0: a later post-order step reads the partial
 //            back), 0}
 //   forward part, child c = 0, 1:  P tile | PT table | row sums
 //   backward part, child c = 0, 1: dP tile | P^T tile | dPT table | dP row sums
-// "tile": a 32 x KD operand tile (tc.cuh layout, TF32-rounded, zero padded) with
+// "tile": a 32 x KD operand tile (tc.cuh layout, TF32 or BF16, zero padded) with
 // row a, column b = M[a][b], so that D = L * tile^T is the Down vector L P^T;
 // the P^T tile holds P[b][a] at (a, b) (pre-order: pt P).  "table": K rows of
 // K4 = K rounded up to 4 FP32 entries, row s = column s of the matrix (the Down
@@ -126,20 +127,33 @@ struct PruneArgs {
 constexpr int TC_M = 128;
 constexpr int TC_N = 32;
 constexpr int TC_HDR = 64;
-__host__ __device__ constexpr int tc_kd(int K) { return (K + 7) / 8 * 8; }
+// operand format: 0 = TF32 (4-byte elements, 8 per MMA K step), 1 = BF16 (2-byte, 16)
+__host__ __device__ constexpr int tc_esz(int fmt) { return fmt ? 2 : 4; }
+__host__ __device__ constexpr int tc_kstep(int fmt) { return fmt ? 16 : 8; }
+__host__ __device__ constexpr int tc_vk(int K) { return (K + 7) / 8 * 8; }   // register vectors
+__host__ __device__ constexpr int tc_kd(int K, int fmt) {                     // operand K extent
+    return (K + tc_kstep(fmt) - 1) / tc_kstep(fmt) * tc_kstep(fmt);
+}
 __host__ __device__ constexpr int tc_k4(int K) { return (K + 3) / 4 * 4; }
-__host__ __device__ constexpr int tc_tile(int K) { return TC_N * tc_kd(K) * 4; }
+__host__ __device__ constexpr int tc_atile(int K, int fmt) { return TC_M * tc_kd(K, fmt) * tc_esz(fmt); }
+__host__ __device__ constexpr int tc_tile(int K, int fmt) { return TC_N * tc_kd(K, fmt) * tc_esz(fmt); }
 __host__ __device__ constexpr int tc_tab(int K) { return K * tc_k4(K) * 4; }
 __host__ __device__ constexpr int tc_rs(int K) { return tc_k4(K) * 4; }
-__host__ __device__ constexpr int tc_fchild(int K) { return tc_tile(K) + tc_tab(K) + tc_rs(K); }
-__host__ __device__ constexpr int tc_bchild(int K) { return 2 * tc_tile(K) + tc_tab(K) + tc_rs(K); }
-__host__ __device__ constexpr int tc_fwd_bytes(int K) { return TC_HDR + 2 * tc_fchild(K); }
-__host__ __device__ constexpr int tc_rec_bytes(int K) { return tc_fwd_bytes(K) + 2 * tc_bchild(K); }
+__host__ __device__ constexpr int tc_fchild(int K, int fmt) { return tc_tile(K, fmt) + tc_tab(K) + tc_rs(K); }
+__host__ __device__ constexpr int tc_bchild(int K, int fmt) {
+    return 2 * tc_tile(K, fmt) + tc_tab(K) + tc_rs(K);
+}
+__host__ __device__ constexpr int tc_fwd_bytes(int K, int fmt) { return TC_HDR + 2 * tc_fchild(K, fmt); }
+__host__ __device__ constexpr int tc_rec_bytes(int K, int fmt) {
+    return tc_fwd_bytes(K, fmt) + 2 * tc_bchild(K, fmt);
+}
 // shared memory of one tensor-core CTA: two stages of (two A tiles, one record
 // buffer), barriers
-__host__ __device__ constexpr int tc_rec_slot(int K) { return (tc_rec_bytes(K) + 127) / 128 * 128; }
-__host__ __device__ constexpr int tc_smem_bytes(int K) {
-    return 4 * TC_M * tc_kd(K) * 4 + 2 * tc_rec_slot(K) + 256;
+__host__ __device__ constexpr int tc_rec_slot(int K, int fmt) {
+    return (tc_rec_bytes(K, fmt) + 127) / 128 * 128;
+}
+__host__ __device__ constexpr int tc_smem_bytes(int K, int fmt) {
+    return 4 * tc_atile(K, fmt) + 2 * tc_rec_slot(K, fmt) + 256;
 }
 
 struct BuildRecArgs {
@@ -929,8 +943,9 @@ struct GatherArgs {
 cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st);
 
 // Tensor-core path (kernels_tc.cu).
-cudaError_t launch_build_records_tc(const BuildRecArgs& a, cudaStream_t st);
-cudaError_t launch_prune_tc(int K, int blocks, const PruneArgs& a, cudaStream_t st);
-cudaError_t occupancy_prune_tc(int K, int* blocks_per_sm);
+// fmt: 0 = TF32, 1 = BF16 operands
+cudaError_t launch_build_records_tc(int fmt, const BuildRecArgs& a, cudaStream_t st);
+cudaError_t launch_prune_tc(int fmt, int K, int blocks, const PruneArgs& a, cudaStream_t st);
+cudaError_t occupancy_prune_tc(int fmt, int K, int* blocks_per_sm);
 
 }  // namespace mcphy

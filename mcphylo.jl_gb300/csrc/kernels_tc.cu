@@ -22,6 +22,8 @@
 
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "kernels.cuh"
 #include "tc.cuh"
 
@@ -52,6 +54,7 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
 // written as row s of the P and dP tiles, column s of the P^T tile and of the two
 // tables, and entry s of the row sums -- zero where s or the column is a padding
 // state; identity for a virtual branch.
+template <int FMT>
 __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, C = a.C;
@@ -64,8 +67,8 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
     const InstanceDesc& d = a.inst[sj.x];
     const int j = sj.y;
     const SchedNode sn = a.sched[d.sched_off + j];
-    const int KD = tc_kd(K), K4 = tc_k4(K);
-    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(tc_rec_bytes(K));
+    const int KD = tc_kd(K, FMT), K4 = tc_k4(K);
+    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(tc_rec_bytes(K, FMT));
     if (c == 0 && s == 0) {
         int* hd = reinterpret_cast<int*>(rec);
         hd[0] = sn.op[0];
@@ -88,17 +91,23 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
         hd[14] = sn.fpush;      // >= 0: a later post-order step reads this partial back
         hd[15] = 0;
     }
-    unsigned char* f = rec + TC_HDR + c * tc_fchild(K);
-    unsigned char* bk = rec + tc_fwd_bytes(K) + c * tc_bchild(K);
+    const int TB = tc_tile(K, FMT);
+    unsigned char* f = rec + TC_HDR + c * tc_fchild(K, FMT);
+    unsigned char* bk = rec + tc_fwd_bytes(K, FMT) + c * tc_bchild(K, FMT);
     unsigned char* Pt = f;
-    float* PTab = reinterpret_cast<float*>(f + tc_tile(K));
-    float* rs = reinterpret_cast<float*>(f + tc_tile(K) + tc_tab(K));
+    float* PTab = reinterpret_cast<float*>(f + TB);
+    float* rs = reinterpret_cast<float*>(f + TB + tc_tab(K));
     unsigned char* dPt = bk;
-    unsigned char* PTt = bk + tc_tile(K);
-    float* dPTab = reinterpret_cast<float*>(bk + 2 * tc_tile(K));
-    float* drs = reinterpret_cast<float*>(bk + 2 * tc_tile(K) + tc_tab(K));
-    auto at = [&](unsigned char* tile, int row, int col) -> float& {
-        return *reinterpret_cast<float*>(tile + tc::tile_off(row, col, KD));
+    unsigned char* PTt = bk + TB;
+    float* dPTab = reinterpret_cast<float*>(bk + 2 * TB);
+    float* drs = reinterpret_cast<float*>(bk + 2 * TB + tc_tab(K));
+    // operand-tile element (row, col) in the tile format (TF32-rounded or BF16)
+    auto put = [&](unsigned char* tile, int row, int col, float v) {
+        if constexpr (FMT == 0)
+            *reinterpret_cast<float*>(tile + tc::tile_off_e<4>(row, col, KD)) = tc::to_tf32(v);
+        else
+            *reinterpret_cast<__nv_bfloat16*>(tile + tc::tile_off_e<2>(row, col, KD)) =
+                __float2bfloat16_rn(v);
     };
     const int b = sn.br[c];
     const bool real = b < d.n_branch;
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
         }
     }
     double row = 0.0, drow = 0.0;
-    float prow[32];
+    float prow[32] = {};
     for (int k = 0; k < KD; ++k) {
         double p = 0.0, dp = 0.0;
         if (s < K && k < K) {
@@ -135,8 +144,8 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
             dPTab[k * K4 + s] = float(dp);
         }
         prow[k] = float(p);
-        at(Pt, s, k) = tc::to_tf32(float(p));
-        at(dPt, s, k) = tc::to_tf32(float(dp));
+        put(Pt, s, k, float(p));
+        put(dPt, s, k, float(dp));
     }
     if (s >= K && s < K4)
         for (int k = 0; k < K; ++k) {
@@ -149,8 +158,7 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
     }
     // column s of the P^T tile: P^T tile (n, s) = P[s][n] -> row n < 32, column s < KD
     if (s < KD)
-        for (int n = 0; n < TC_N; ++n)
-            at(PTt, n, s) = tc::to_tf32((n < K && s < K) ? prow[n] : 0.f);
+        for (int n = 0; n < TC_N; ++n) put(PTt, n, s, (n < K && s < K) ? prow[n] : 0.f);
 }
 
 // ---------------------------------------------------------------- device helpers
@@ -205,14 +213,31 @@ __device__ __forceinline__ void dot2(const float (&pt)[KD], const float (&x)[KD]
     ny = (ay[0] + ay[1]) + (ay[2] + ay[3]);
 }
 
-// This thread's row of an A tile (TF32-rounded).
-template <int KD>
-__device__ __forceinline__ void write_a(unsigned char* tile, int row, const float (&v)[KD]) {
+// This thread's row of an A tile: VK values, zero beyond (TF32-rounded or BF16).
+template <int VK, int FMT>
+__device__ __forceinline__ void write_a(unsigned char* tile, int row, const float (&v)[VK]) {
+    if constexpr (FMT == 0) {
 #pragma unroll
-    for (int k = 0; k < KD; k += 4)
-        *reinterpret_cast<float4*>(tile + tc::tile_off(row, k, KD)) =
-            make_float4(tc::to_tf32(v[k]), tc::to_tf32(v[k + 1]), tc::to_tf32(v[k + 2]),
-                        tc::to_tf32(v[k + 3]));
+        for (int k = 0; k < VK; k += 4)
+            *reinterpret_cast<float4*>(tile + tc::tile_off_e<4>(row, k, VK)) =
+                make_float4(tc::to_tf32(v[k]), tc::to_tf32(v[k + 1]), tc::to_tf32(v[k + 2]),
+                            tc::to_tf32(v[k + 3]));
+    } else {
+        constexpr int KD = (VK + 15) / 16 * 16;
+#pragma unroll
+        for (int k = 0; k < KD; k += 8) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float lo = (k + 2 * q < VK) ? v[k + 2 * q < VK ? k + 2 * q : 0] : 0.f;
+                const float hi = (k + 2 * q + 1 < VK) ? v[k + 2 * q + 1 < VK ? k + 2 * q + 1 : 0] : 0.f;
+                const __nv_bfloat162 pr = __floats2bfloat162_rn(lo, hi);
+                w[q] = *reinterpret_cast<const uint32_t*>(&pr);
+            }
+            *reinterpret_cast<uint4*>(tile + tc::tile_off_e<2>(row, k, KD)) =
+                make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
 }
 
 // KD columns of this thread's TMEM lane from column `taddr` (loads and the wait in
@@ -245,15 +270,18 @@ __device__ __forceinline__ void col_store(float* col, int slot, int K, int t, co
 // Stage s (two, alternating by step): the step's record (forward: its first part)
 // and the A tiles of its internal children, on one mbarrier, issued two steps
 // ahead from the lookahead fields of the step record headers.
-template <int KD>
+template <int VK, int FMT>
 __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
-    constexpr int TILE = TC_M * KD * 4;           // bytes of one A tile
+    constexpr int ESZ = FMT ? 2 : 4;                  // operand element bytes
+    constexpr int KSTEP = FMT ? 16 : 8;               // K of one MMA instruction
+    constexpr int KD = (VK + KSTEP - 1) / KSTEP * KSTEP;   // operand K extent
+    constexpr int TILE = TC_M * KD * ESZ;             // bytes of one A tile
     extern __shared__ __align__(1024) unsigned char sm[];
     const int K = a.K, K4 = tc_k4(a.K), C = a.C;
-    const int RB = tc_rec_bytes(K), FB = tc_fwd_bytes(K);
+    const int RB = tc_rec_bytes(K, FMT), FB = tc_fwd_bytes(K, FMT);
     unsigned char* T = sm;                                       // [stage][child] A tiles
     unsigned char* Rb = sm + 4 * TILE;                            // [stage] records
-    uint64_t* bars = reinterpret_cast<uint64_t*>(Rb + 2 * tc_rec_slot(K));   // st0, st1, mma
+    uint64_t* bars = reinterpret_cast<uint64_t*>(Rb + 2 * tc_rec_slot(K, FMT));   // st0, st1, mma
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 3);
     int* item_sh = reinterpret_cast<int*>(tslot + 1);
     float* red = reinterpret_cast<float*>(item_sh + 3);            // [2][4 warps][2]
@@ -275,8 +303,8 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
     tc::fence_after_sync();
     const uint32_t tbase = *tslot;
     const uint32_t tl = tbase + (uint32_t(warp * 32) << 16);     // this warp's lane quarter
-    const uint32_t idesc = tc::idesc_tf32(TC_M, TC_N);
-    const uint32_t sbo = uint32_t(tc::tile_sbo(KD));
+    const uint32_t idesc = FMT ? tc::idesc_bf16(TC_M, TC_N) : tc::idesc_tf32(TC_M, TC_N);
+    const uint32_t sbo = uint32_t(tc::tile_sbo_e<ESZ>(KD));
     unsigned char* post = reinterpret_cast<unsigned char*>(a.post) +
                           size_t(blockIdx.x) * size_t(a.warp_stride) * 4;
     float* pre = reinterpret_cast<float*>(a.pre) + int64_t(blockIdx.x) * a.pre_warp_stride;
@@ -289,7 +317,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
     bool failed = false;
 
     auto tile = [&](int st, int c) { return T + (2 * st + c) * TILE; };
-    auto rec = [&](int st) { return Rb + st * tc_rec_slot(K); };
+    auto rec = [&](int st) { return Rb + st * tc_rec_slot(K, FMT); };
     // thread 0: one step's copies on stage st -- its record (rec_bytes of it) and the
     // post-order tiles of its internal children (op < 0: a leaf, nothing to copy)
     auto issue = [&](int st, const unsigned char* src, int rec_bytes, int op0, int op1) {
@@ -325,10 +353,12 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             for (int i = 0; i < n; ++i) {
                 const uint32_t a0 = tc::smem_addr(at[i]), b0 = tc::smem_addr(bt[i]);
 #pragma unroll
-                for (int s = 0; s < KD / 8; ++s)
-                    tc::mma_tf32(tbase + dcol[i], tc::smem_desc(a0 + 256u * s, tc::kCoreBytes, sbo),
-                                 tc::smem_desc(b0 + 256u * s, tc::kCoreBytes, sbo), idesc,
-                                 s > 0 ? 1u : 0u);
+                for (int s = 0; s < KD / KSTEP; ++s) {
+                    const uint64_t ad = tc::smem_desc(a0 + 256u * s, tc::kCoreBytes, sbo);
+                    const uint64_t bd = tc::smem_desc(b0 + 256u * s, tc::kCoreBytes, sbo);
+                    if constexpr (FMT == 0) tc::mma_tf32(tbase + dcol[i], ad, bd, idesc, s > 0 ? 1u : 0u);
+                    else tc::mma_bf16(tbase + dcol[i], ad, bd, idesc, s > 0 ? 1u : 0u);
+                }
             }
             tc::mma_commit(bars + 2);
             mma_pend = true;
@@ -373,7 +403,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         }
         uint32_t eacc = 0u;
         double ll = 0.0;
-        float Lp[KD];
+        float Lp[VK];
         zero(Lp);
         for (int j = 0; j < J; ++j) {
             const int b = j & 1;
@@ -381,12 +411,12 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             const int* hd = reinterpret_cast<const int*>(R);
             const int op0 = hd[0], op1 = hd[1];
             const unsigned char* f0 = R + TC_HDR;
-            const unsigned char* f1 = f0 + tc_fchild(K);
+            const unsigned char* f1 = f0 + tc_fchild(K, FMT);
             // leaf codes of the next step, one step ahead
             const uint32_t ncode0 = (j + 1 < J) ? code_of(hd[6]) : 0u;
             const uint32_t ncode1 = (j + 1 < J) ? code_of(hd[7]) : 0u;
-            if (op1 >= 0) write_a<KD>(tile(b, 1), t, Lp);   // op1 == j - 1: the carried partial
-            float D0[KD], D1[KD];
+            if (op1 >= 0) write_a<VK, FMT>(tile(b, 1), t, Lp);   // op1 == j - 1: the carried partial
+            float D0[VK], D1[VK];
             bool ok = true;
             if (op0 >= 0 || op1 >= 0) {
                 const unsigned char* at[2];
@@ -397,24 +427,24 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = f1; dc[n] = 64; ++n; }
                 ok = mma_round(n, at, bt, dc);
                 if (ok) {
-                    if (op0 >= 0) tmem_row<KD>(tl + 0, D0);
-                    if (op1 >= 0) tmem_row<KD>(tl + 64, D1);
+                    if (op0 >= 0) tmem_row<VK>(tl + 0, D0);
+                    if (op1 >= 0) tmem_row<VK>(tl + 64, D1);
                 }
             }
             if (op0 < 0)
-                leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
+                leaf_down<VK>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K, FMT)),
+                              reinterpret_cast<const float*>(f0 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D0);
             if (op1 < 0)
-                leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
+                leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
+                              reinterpret_cast<const float*>(f1 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D1);
 #pragma unroll
             for (int k = 0; k < KD; ++k) D0[k] *= D1[k];
-            eacc += rescale<KD, float>(D0);
+            eacc += rescale<VK, float>(D0);
             if (j + 1 < J) {
                 // TF32 copy in operand layout for the steps that read it back; the
                 // copies a later post-order step reads by TMA are fenced now, the
                 // rest once before the gradient sweep
-                write_a<KD>(post + size_t(j) * TILE, t, D0);
+                write_a<VK, FMT>(post + size_t(j) * TILE, t, D0);
                 if (hd[14] >= 0) fence_proxy_async_global();
 #pragma unroll
                 for (int k = 0; k < KD; ++k) Lp[k] = D0[k];
@@ -478,8 +508,8 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 at[n] = tile(st, 0); bt[n] = q0; dc[n] = 32; ++n;
             }
             if (h[1] >= 0) {
-                at[n] = tile(st, 1); bt[n] = g0 + tc_fchild(K); dc[n] = 64; ++n;
-                at[n] = tile(st, 1); bt[n] = q0 + tc_bchild(K); dc[n] = 96; ++n;
+                at[n] = tile(st, 1); bt[n] = g0 + tc_fchild(K, FMT); dc[n] = 64; ++n;
+                at[n] = tile(st, 1); bt[n] = q0 + tc_bchild(K, FMT); dc[n] = 96; ++n;
             }
         };
         bool okr;
@@ -491,7 +521,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             if (t == 0) add_round1(0, n, at, bt, dc);
             okr = mma_round(n, at, bt, dc);
         }
-        float pb[KD];
+        float pb[VK];
 #pragma unroll
         for (int k = 0; k < KD; ++k) pb[k] = (k < K) ? float(__ldg(pi_d + k)) : 0.f;
         for (int j = J - 1; j >= 0; --j) {
@@ -501,65 +531,65 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             const int op0 = hd[0], op1 = hd[1], bpush = hd[2];
             const int gr0 = hd[4], gr1 = hd[5];
             const unsigned char* f0 = R + TC_HDR;
-            const unsigned char* f1 = f0 + tc_fchild(K);
+            const unsigned char* f1 = f0 + tc_fchild(K, FMT);
             const unsigned char* k0 = R + FB;
-            const unsigned char* k1 = k0 + tc_bchild(K);
+            const unsigned char* k1 = k0 + tc_bchild(K, FMT);
             // next step's leaf codes and stacked pre-order partial, one step ahead
             uint32_t ncode0 = 0u, ncode1 = 0u;
-            float pbn[KD];
+            float pbn[VK];
             zero(pbn);
             if (j > 0) {
                 ncode0 = code_of(hd[9]);
                 ncode1 = code_of(hd[10]);
-                if (hd[11] >= 0) col_load<KD>(pre, hd[11], K, t, pbn);
+                if (hd[11] >= 0) col_load<VK>(pre, hd[11], K, t, pbn);
             }
             // Down vectors of both children (TMEM for internal ones, tables for leaves)
-            float D0[KD], D1[KD];
+            float D0[VK], D1[VK];
             if (op0 >= 0) {
-                if (okr) tmem_row<KD>(tl + 0, D0);
+                if (okr) tmem_row<VK>(tl + 0, D0);
             } else {
-                leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f0 + tc_tile(K) + tc_tab(K)), K, K4, D0);
+                leaf_down<VK>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K, FMT)),
+                              reinterpret_cast<const float*>(f0 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D0);
             }
             if (op1 >= 0) {
-                if (okr) tmem_row<KD>(tl + 64, D1);
+                if (okr) tmem_row<VK>(tl + 64, D1);
             } else {
-                leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K)),
-                              reinterpret_cast<const float*>(f1 + tc_tile(K) + tc_tab(K)), K, K4, D1);
+                leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
+                              reinterpret_cast<const float*>(f1 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D1);
             }
             // child 1: pt_1 = pb * D_0; child 0: pt_0 = pb * D_1
             float g0, g1;
             {
-                float pt[KD], dD[KD];
+                float pt[VK], dD[VK];
                 if (op1 >= 0) {
-                    if (okr) tmem_row<KD>(tl + 96, dD);
+                    if (okr) tmem_row<VK>(tl + 96, dD);
                 } else {
-                    leaf_down<KD>(code1, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K)),
-                                  reinterpret_cast<const float*>(k1 + 2 * tc_tile(K) + tc_tab(K)), K,
+                    leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K, FMT)),
+                                  reinterpret_cast<const float*>(k1 + 2 * tc_tile(K, FMT) + tc_tab(K)), K,
                                   K4, dD);
                 }
 #pragma unroll
                 for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D0[k];
                 float num, den;
-                dot2<KD>(pt, dD, D1, num, den);
+                dot2<VK>(pt, dD, D1, num, den);
                 g1 = valid ? __fdividef(num, den) : 0.f;
-                if (op1 >= 0) write_a<KD>(tile(b, 1), t, pt);
+                if (op1 >= 0) write_a<VK, FMT>(tile(b, 1), t, pt);
             }
             {
-                float pt[KD], dD[KD];
+                float pt[VK], dD[VK];
                 if (op0 >= 0) {
-                    if (okr) tmem_row<KD>(tl + 32, dD);
+                    if (okr) tmem_row<VK>(tl + 32, dD);
                 } else {
-                    leaf_down<KD>(code0, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K)),
-                                  reinterpret_cast<const float*>(k0 + 2 * tc_tile(K) + tc_tab(K)), K,
+                    leaf_down<VK>(code0, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K, FMT)),
+                                  reinterpret_cast<const float*>(k0 + 2 * tc_tile(K, FMT) + tc_tab(K)), K,
                                   K4, dD);
                 }
 #pragma unroll
                 for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D1[k];
                 float num, den;
-                dot2<KD>(pt, dD, D0, num, den);
+                dot2<VK>(pt, dD, D0, num, den);
                 g0 = valid ? __fdividef(num, den) : 0.f;
-                if (op0 >= 0) write_a<KD>(tile(b, 0), t, pt);
+                if (op0 >= 0) write_a<VK, FMT>(tile(b, 0), t, pt);
             }
             g0 = warp_sum(g0);
             g1 = warp_sum(g1);
@@ -580,8 +610,8 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 uint32_t dc[6];
                 int n = 0;
                 if (t == 0) {
-                    if (op0 >= 0) { at[n] = tile(b, 0); bt[n] = k0 + tc_tile(K); dc[n] = 128; ++n; }
-                    if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = k1 + tc_tile(K); dc[n] = 160; ++n; }
+                    if (op0 >= 0) { at[n] = tile(b, 0); bt[n] = k0 + tc_tile(K, FMT); dc[n] = 128; ++n; }
+                    if (op1 >= 0) { at[n] = tile(b, 1); bt[n] = k1 + tc_tile(K, FMT); dc[n] = 160; ++n; }
                     if (next_in) add_round1(b ^ 1, n, at, bt, dc);
                 }
                 okr = mma_round(n, at, bt, dc);
@@ -589,14 +619,14 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             ok = ok && okr;
             if (okr) {
                 if (op0 >= 0) {
-                    float P0[KD];
-                    tmem_row<KD>(tl + 128, P0);
-                    rescale<KD, float>(P0);
-                    col_store<KD>(pre, bpush, K, t, P0);
+                    float P0[VK];
+                    tmem_row<VK>(tl + 128, P0);
+                    rescale<VK, float>(P0);
+                    col_store<VK>(pre, bpush, K, t, P0);
                 }
                 if (op1 >= 0) {
-                    tmem_row<KD>(tl + 160, pbn);        // step j - 1's own partial: carried
-                    rescale<KD, float>(pbn);
+                    tmem_row<VK>(tl + 160, pbn);        // step j - 1's own partial: carried
+                    rescale<VK, float>(pbn);
                 }
             }
 #pragma unroll
@@ -636,36 +666,36 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
     if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
-template <int KD>
+template <int VK, int FMT>
 cudaError_t go_tc(int blocks, const PruneArgs& a, cudaStream_t st) {
-    const int smem = tc_smem_bytes(a.K);
+    const int smem = tc_smem_bytes(a.K, FMT);
     static int configured = 0;
     if (smem > configured) {
         cudaError_t e =
-            cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  100);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    prune_tc_kernel<KD><<<blocks, TC_M, smem, st>>>(a);
+    prune_tc_kernel<VK, FMT><<<blocks, TC_M, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int KD>
+template <int VK, int FMT>
 cudaError_t occ_tc(int K, int* bps) {
-    const int smem = tc_smem_bytes(K);
+    const int smem = tc_smem_bytes(K, FMT);
     cudaError_t e =
-        cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(prune_tc_kernel<KD>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    e = cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     // resident CTAs per SM from the kernel's own limits: registers (allocated per
     // warp in units of 256), shared memory (plus the 1 KB each CTA reserves) and
     // TMEM (512 columns per SM)
     cudaFuncAttributes fa{};
-    e = cudaFuncGetAttributes(&fa, prune_tc_kernel<KD>);
+    e = cudaFuncGetAttributes(&fa, prune_tc_kernel<VK, FMT>);
     if (e != cudaSuccess) return e;
     int dev = 0, regs_sm = 0, smem_sm = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -684,28 +714,36 @@ cudaError_t occ_tc(int K, int* bps) {
 
 }  // namespace
 
-cudaError_t launch_build_records_tc(const BuildRecArgs& a, cudaStream_t st) {
+cudaError_t launch_build_records_tc(int fmt, const BuildRecArgs& a, cudaStream_t st) {
     const int64_t total = int64_t(a.n_steps) * 2 * a.C * TC_N;
     if (total == 0) return cudaSuccess;
     const int tpb = 128;
-    build_records_tc_kernel<<<unsigned((total + tpb - 1) / tpb), tpb, 0, st>>>(a);
+    const unsigned blocks = unsigned((total + tpb - 1) / tpb);
+    if (fmt) build_records_tc_kernel<1><<<blocks, tpb, 0, st>>>(a);
+    else build_records_tc_kernel<0><<<blocks, tpb, 0, st>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_prune_tc(int K, int blocks, const PruneArgs& a, cudaStream_t st) {
-    switch (tc_kd(K)) {
-        case 16: return go_tc<16>(blocks, a, st);
-        case 24: return go_tc<24>(blocks, a, st);
-        case 32: return go_tc<32>(blocks, a, st);
+cudaError_t launch_prune_tc(int fmt, int K, int blocks, const PruneArgs& a, cudaStream_t st) {
+    switch (tc_vk(K) * 2 + (fmt ? 1 : 0)) {
+        case 32: return go_tc<16, 0>(blocks, a, st);
+        case 33: return go_tc<16, 1>(blocks, a, st);
+        case 48: return go_tc<24, 0>(blocks, a, st);
+        case 49: return go_tc<24, 1>(blocks, a, st);
+        case 64: return go_tc<32, 0>(blocks, a, st);
+        case 65: return go_tc<32, 1>(blocks, a, st);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t occupancy_prune_tc(int K, int* bps) {
-    switch (tc_kd(K)) {
-        case 16: return occ_tc<16>(K, bps);
-        case 24: return occ_tc<24>(K, bps);
-        case 32: return occ_tc<32>(K, bps);
+cudaError_t occupancy_prune_tc(int fmt, int K, int* bps) {
+    switch (tc_vk(K) * 2 + (fmt ? 1 : 0)) {
+        case 32: return occ_tc<16, 0>(K, bps);
+        case 33: return occ_tc<16, 1>(K, bps);
+        case 48: return occ_tc<24, 0>(K, bps);
+        case 49: return occ_tc<24, 1>(K, bps);
+        case 64: return occ_tc<32, 0>(K, bps);
+        case 65: return occ_tc<32, 1>(K, bps);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -24,11 +24,20 @@ namespace tc {
 
 constexpr int kCoreBytes = 128;
 
+// 32-bit elements (TF32): 4 per 16-byte core-matrix row
 __host__ __device__ constexpr int tile_sbo(int kd) { return (kd / 4) * kCoreBytes; }
 __host__ __device__ constexpr int tile_bytes(int rows, int kd) { return rows * kd * 4; }
 // byte offset of element (row, k) in a tile of KD columns
 __host__ __device__ constexpr int tile_off(int row, int k, int kd) {
     return (row >> 3) * tile_sbo(kd) + (k >> 2) * kCoreBytes + (row & 7) * 16 + (k & 3) * 4;
+}
+// the same layout for ESZ-byte elements (2: BF16, 8 per core-matrix row)
+template <int ESZ> __host__ __device__ constexpr int tile_sbo_e(int kd) {
+    return (kd * ESZ / 16) * kCoreBytes;
+}
+template <int ESZ> __host__ __device__ constexpr int tile_off_e(int row, int k, int kd) {
+    return (row >> 3) * tile_sbo_e<ESZ>(kd) + (k / (16 / ESZ)) * kCoreBytes + (row & 7) * 16 +
+           (k % (16 / ESZ)) * ESZ;
 }
 
 // Shared-memory matrix descriptor (64 bit): start address >> 4 in bits [0,14),
@@ -49,6 +58,10 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 // [10,13), N >> 3 in [17,23), M >> 4 in [24,29).
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+// kind::f16 with BF16 operands (format 1) and FP32 accumulation, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -82,6 +95,16 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint6
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+// The same with BF16 operands: M x N x 16 (kind::f16).
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                         uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
         ::"r"(d_tmem), "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate) : "memory");
 }
 

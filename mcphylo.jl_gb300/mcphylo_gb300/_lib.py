@@ -19,6 +19,7 @@ ERR_ARG, ERR_SHAPE, ERR_TREE, ERR_OOM, ERR_CUDA, ERR_STATE, ERR_TIMEOUT, ERR_NO_
 PREC_F32 = 0
 PREC_F64 = 1
 PREC_TF32 = 2
+PREC_BF16 = 3
 
 i64 = ctypes.c_int64
 c_int = ctypes.c_int
@@ -54,7 +55,7 @@ SIGNATURES = {
     "mcphy_logpdf_device": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_logpdf_grad_noalloc": (c_int, [handle_t, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
-    "mcphy_tc_selftest": (c_int, [ctypes.c_int64, ctypes.c_int64, P(ctypes.c_float),
+    "mcphy_tc_selftest": (c_int, [ctypes.c_int64, ctypes.c_int64, c_int, P(ctypes.c_float),
                                   P(ctypes.c_float), P(ctypes.c_float)]),
     "mcphy_set_stream": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_synchronize": (c_int, [handle_t]),

@@ -9,14 +9,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _tc(kd, n, a, b):
+def _tc(kd, n, a, b, bf16=0):
     from mcphylo_gb300 import _lib
     L = _lib.load()
     a = np.ascontiguousarray(a, dtype=np.float32)
     b = np.ascontiguousarray(b, dtype=np.float32)
     d = np.zeros((128, n), dtype=np.float32)
     fp = ctypes.POINTER(ctypes.c_float)
-    st = L.mcphy_tc_selftest(kd, n, a.ctypes.data_as(fp), b.ctypes.data_as(fp),
+    st = L.mcphy_tc_selftest(kd, n, bf16, a.ctypes.data_as(fp), b.ctypes.data_as(fp),
                              d.ctypes.data_as(fp))
     assert st == 0, st
     return d
@@ -37,6 +37,15 @@ def test_exact_small_integers(built_lib, kd, n):
     a = rng.integers(-3, 4, size=(128, kd)).astype(np.float32)
     b = rng.integers(-3, 4, size=(n, kd)).astype(np.float32)
     d = _tc(kd, n, a, b)
+    np.testing.assert_array_equal(d, a.astype(np.float64) @ b.astype(np.float64).T)
+
+
+@pytest.mark.parametrize("kd,n", [(16, 16), (32, 32), (48, 32), (64, 64)])
+def test_exact_small_integers_bf16(built_lib, kd, n):
+    rng = np.random.default_rng(kd * 10 + n)
+    a = rng.integers(-3, 4, size=(128, kd)).astype(np.float32)
+    b = rng.integers(-3, 4, size=(n, kd)).astype(np.float32)
+    d = _tc(kd, n, a, b, bf16=1)
     np.testing.assert_array_equal(d, a.astype(np.float64) @ b.astype(np.float64).T)
 
 
@@ -65,9 +74,9 @@ TF32_LL_RTOL = 5e-4
 TF32_G_RTOL = 5e-3
 
 
-def _tf32_engine(inst):
+def _tf32_engine(inst, precision="tf32"):
     import mcphylo_gb300 as mp
-    e = mp.Engine(inst.K, len(inst.rates), "tf32")
+    e = mp.Engine(inst.K, len(inst.rates), precision)
     e.set_tree(inst.parent, inst.blen)
     e.set_codes(inst.codes, inst.leaf_nums)
     e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
@@ -170,3 +179,26 @@ def test_tf32_rejects_small_state_spaces(built_lib):
     import mcphylo_gb300 as mp
     with pytest.raises(Exception):
         mp.Engine(4, 4, "tf32")
+
+
+# BF16 keeps 8 significant bits: a relative error of up to 2^-9 per rounded operand
+# and node.  Stated tolerances of the BF16 tensor-core path against the FP64 oracle
+# (measured values in the test output): total logL 5e-3 relative, gradient 5e-2 of
+# max|g|.
+BF16_LL_RTOL = 5e-3
+BF16_G_RTOL = 5e-2
+
+
+@pytest.mark.parametrize("K,C,taxa,S,mf", [(20, 4, 24, 300, 0.0), (12, 2, 30, 200, 0.2),
+                                         (32, 1, 10, 70, 0.0)])
+def test_bf16_vs_oracle(built_lib, K, C, taxa, S, mf):
+    inst = random_instance(K, C, taxa, S, seed=K * 11 + taxa, multifurcate=mf)
+    llo, go = oracle(inst)
+    e = _tf32_engine(inst, "bf16")
+    ll, g = e.logpdf_grad()
+    rel = abs(ll - llo) / abs(llo)
+    gerr = np.max(np.abs(g - go)) / np.max(np.abs(go))
+    print(f"bf16 K={K} N={inst.N} S={S}: logL rel {rel:.2e}, grad {gerr:.2e}")
+    assert rel <= BF16_LL_RTOL
+    assert gerr <= BF16_G_RTOL
+    assert e.logpdf() == pytest.approx(ll, rel=1e-12)
