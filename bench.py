@@ -83,25 +83,27 @@ def make_engine(insts, precision, tiles=None):
     return e
 
 
-def tc_algorithmic_bytes(insts, grad=True):
+def tc_algorithmic_bytes(insts, grad=True, bf16=False):
     """Bytes the tensor-core kernel must move per evaluation: every post-order partial
-    of an internal non-root step written once (as a TF32 operand tile, KD entries
-    per site) and read once by the gradient sweep, the leaf state codes read once
-    (4 bytes), the per-item gradient partials written once."""
+    of an internal non-root step written once (as an operand tile, KD entries per
+    site, 4 bytes in TF32 and 2 in BF16) and read once by the gradient sweep, the leaf
+    state codes read once (4 bytes), the per-item gradient partials written once."""
     import mcphylo_gb300 as mp
     total = 0
+    step = 16 if bf16 else 8
+    esz = 2 if bf16 else 4
     for b in insts:
-        KD = (b.K + 7) // 8 * 8
+        KD = (b.K + step - 1) // step * step
         info = mp.schedule_info(b.parent)
         C = len(b.rates)
         blocks = -(-b.S // 128)
         lanes = blocks * 128 * C
         total += len(b.leaf_nums) * b.S * 4
         if grad:
-            total += 2 * lanes * (info["internal"] - 1) * KD * 4
+            total += 2 * lanes * (info["internal"] - 1) * KD * esz
             total += C * blocks * (b.N - 1) * 4
         else:
-            total += lanes * (info["internal"] - 1) * KD * 4
+            total += lanes * (info["internal"] - 1) * KD * esz
     return total
 
 
@@ -436,8 +438,9 @@ def run_gpu(args, rank, world):
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
 
     prec = args.precision
-    if prec == "tf32" and insts[0].K < 9:
-        raise SystemExit("--precision tf32 is the dense-state path (K >= 9)")
+    tc_path = prec in ("tf32", "bf16")
+    if tc_path and insts[0].K < 9:
+        raise SystemExit("--precision tf32/bf16 is the dense-state path (K >= 9)")
     if args.tiles == "auto":
         # the library's autotuner: times each launch shape on this problem
         e = make_engine(insts, prec)
@@ -584,7 +587,7 @@ def run_gpu(args, rank, world):
 
     # the SIMT FP32 path on the same inputs, beside the tensor-core one
     simt = None
-    if prec == "tf32":
+    if tc_path:
         e32 = make_engine(insts, "f32")
         e32.autotune()
         e32.enable_timing(True)
@@ -603,9 +606,9 @@ def run_gpu(args, rank, world):
         e32.close()
 
     real_b = 4
-    if prec == "tf32":
-        alg = tc_algorithmic_bytes(insts, args.mode == "grad")
-        kname = "prune_tc_kernel<%d>" % ((insts[0].K + 7) // 8 * 8)
+    if tc_path:
+        alg = tc_algorithmic_bytes(insts, args.mode == "grad", prec == "bf16")
+        kname = "prune_tc_kernel<%d,%s>" % ((insts[0].K + 7) // 8 * 8, prec)
     else:
         alg = algorithmic_bytes(insts, tiles[0], real_b, args.mode == "grad")
         kname = "prune_kernel<4,float,%d>" % tiles[0]
@@ -620,7 +623,7 @@ def run_gpu(args, rank, world):
         try:
             tj = json.load(open(tpath))
             tj = tj.get(kname, tj) if isinstance(tj, dict) else tj
-            if tj.get("kernel") == kname and (prec == "tf32" or insts[0].K == 4):
+            if tj.get("kernel") == kname and (tc_path or insts[0].K == 4):
                 traffic = float(tj["bytes_per_unit"]) * units
                 traffic_note = (f"ncu dram bytes of a {tj['captured_workload']} launch scaled by "
                                 f"units ({tj['bytes_per_unit']} B/unit)")
@@ -646,7 +649,7 @@ def run_gpu(args, rank, world):
         "logL-only site-node updates/s, FP32-scaled vs plain FP64 GPU at ≤1e-6 rel err"
     out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "tf32" if prec == "tf32" else "f32",
+           "vs_baseline": None, "dtype": prec,
            "data": "synthetic (seeded simulation down Yule trees)",
            "config": dict(cfg, tiles={"sites_per_thread": tiles[0], "threads_per_block": tiles[1]},
                           l2="flushed between steps (512 MB write, outside the timed events)",
@@ -681,8 +684,9 @@ def main():
     ap.add_argument("--nuts-adapt", type=int, default=200)
     ap.add_argument("--nuts-seed", type=int, default=1)
     ap.add_argument("--nuts-target", type=float, default=0.8)
-    ap.add_argument("--precision", default="f32", choices=["f32", "tf32"],
-                    help="f32: FP32-scaled SIMT path; tf32: tensor-core node updates (K >= 9)")
+    ap.add_argument("--precision", default="f32", choices=["f32", "tf32", "bf16"],
+                    help="f32: FP32-scaled SIMT path; tf32 / bf16: tensor-core node updates "
+                         "with TF32 / BF16 operands (K >= 9)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
