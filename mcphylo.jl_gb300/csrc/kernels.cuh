@@ -261,6 +261,38 @@ __device__ __forceinline__ uint32_t rescale(Real (&v)[KP]) {
     return field;
 }
 
+// Lazy rescale of a warp's partials: only when the maximum of some site in the
+// warp has fallen below 2^-32 (FP32) / 2^-256 (FP64) -- a warp-uniform branch -- so
+// values stay normal (partials only shrink down the tree: P's rows sum to one) and
+// most steps skip the work.  acc[u] gains the biased exponent field of site u's
+// rescale, or the bias itself (exponent 0) when the warp skipped it.
+template <typename Real> struct LazyLow;
+template <> struct LazyLow<float> { static constexpr float value = 0x1p-32f; };
+template <> struct LazyLow<double> { static constexpr double value = 0x1p-256; };
+
+template <int KP, typename Real, int SPT>
+__device__ __forceinline__ void rescale_warp(Real (&v)[SPT][KP], uint32_t (&acc)[SPT]) {
+    Real m[SPT];
+    bool low = false;
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) {
+        m[u] = vmax<KP, Real>(v[u]);
+        low = low || !(m[u] >= LazyLow<Real>::value);
+    }
+    if (__any_sync(0xffffffffu, low)) {
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) {
+            Real f;
+            acc[u] += scale_bits(m[u], f);
+#pragma unroll
+            for (int k = 0; k < KP; ++k) v[u][k] *= f;
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) acc[u] += ExpBias<Real>::value;
+    }
+}
+
 // KP Reals from global or shared memory with the widest aligned vector access.
 template <int KP, typename Real>
 __device__ __forceinline__ void ld_vec(const Real* p, Real (&v)[KP]) {
@@ -683,11 +715,10 @@ prune_kernel(const PruneArgs a) {
             down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), Da);
             down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), Db);
 #pragma unroll
-            for (int u = 0; u < SPT; ++u) {
+            for (int u = 0; u < SPT; ++u)
 #pragma unroll
                 for (int k = 0; k < KP; ++k) Da[u][k] *= Db[u][k];
-                eacc[u] += rescale<KP>(Da[u]);
-            }
+            rescale_warp<KP, Real, SPT>(Da, eacc);
             if (j + 1 < J) {
                 // the post-order column is only read back by the gradient sweep
                 if (a.want_grad) write_vec<KP, SPT>(post + int64_t(j) * SLOT, lane, Da);
@@ -796,8 +827,8 @@ prune_kernel(const PruneArgs a) {
                 if (h[c] >= 0) {
                     Real pbc[SPT][KP];
                     apply_tt<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 2 * c), pt, pbc);
-#pragma unroll
-                    for (int u = 0; u < SPT; ++u) rescale<KP>(pbc[u]);
+                    uint32_t unused[SPT] = {};
+                    rescale_warp<KP, Real, SPT>(pbc, unused);
                     if (c == 1) copy_part(Npb, pbc);                             // step j-1
                     else write_vec<KP, SPT>(stack_ptr(h[2]), lane, pbc);
                 }
