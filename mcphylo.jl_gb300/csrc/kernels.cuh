@@ -601,8 +601,10 @@ __device__ __forceinline__ void down(const Real (&L)[SPT][KP], bool code_leaf, b
 __device__ __forceinline__ float ratio(float n, float d) { return __fdividef(n, d); }
 __device__ __forceinline__ double ratio(double n, double d) { return n / d; }
 
-__device__ __forceinline__ float log_real(float x) { return logf(x); }
-__device__ __forceinline__ double log_real(double x) { return log(x); }
+// Site log-likelihood of the root sum, in FP64: with lazy rescaling the root sum can
+// lie far below 1, where an FP32 logarithm would lose absolute accuracy.
+__device__ __forceinline__ double log_site(float x) { return log(double(x)); }
+__device__ __forceinline__ double log_site(double x) { return log(x); }
 
 template <int SPT, int KP, typename Real>
 __device__ __forceinline__ void copy_part(Real (&dst)[SPT][KP], const Real (&src)[SPT][KP]) {
@@ -731,7 +733,7 @@ prune_kernel(const PruneArgs a) {
 #pragma unroll
                     for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Da[u][k], lik);
                     const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
-                    const double v = double(log_real(lik)) + double(ex) * LN2;
+                    const double v = log_site(lik) + double(ex) * LN2;
                     ll_lane += valid[u] ? v : 0.0;
                 }
             }
