@@ -39,8 +39,10 @@ def test_simudata_gradient_golden(built_lib, golden, precision, rtol, floor):
     pd, x, g = _golden_pd(golden, "simudata", precision)
     ll, grad = mp.gradlogpdf(pd, x)
     assert_grad_close(grad, g["grad"], rtol, floor)
-    # the reference's own ll golden is only good to its isapprox tolerance
-    assert abs(ll - g["ll"]) <= 1.5e-8 * abs(g["ll"])
+    # the reference's own ll golden is only good to its isapprox tolerance (sqrt eps);
+    # the FP32 path is held to its own logL tolerance
+    tol = 1.5e-8 if precision == "f64" else F32_LL_RTOL
+    assert abs(ll - g["ll"]) <= tol * abs(g["ll"])
 
 
 def test_multiplephylodist_golden(built_lib, golden):
