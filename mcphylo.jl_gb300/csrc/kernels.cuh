@@ -261,8 +261,8 @@ __device__ __forceinline__ uint32_t rescale(Real (&v)[KP]) {
     return field;
 }
 
-// Lazy rescale of a warp's partials: only when the maximum of some site in the
-// warp has fallen below 2^-32 (FP32) / 2^-256 (FP64) -- a warp-uniform branch -- so
+// Lazy rescale of a warp's FP64 partials: only when the maximum of some site in the
+// warp has fallen below 2^-256 -- a warp-uniform branch -- so
 // values stay normal (partials only shrink down the tree: P's rows sum to one) and
 // most steps skip the work.  acc[u] gains the biased exponent field of site u's
 // rescale, or the bias itself (exponent 0) when the warp skipped it.
@@ -272,6 +272,12 @@ template <> struct LazyLow<double> { static constexpr double value = 0x1p-256; }
 
 template <int KP, typename Real, int SPT>
 __device__ __forceinline__ void rescale_warp(Real (&v)[SPT][KP], uint32_t (&acc)[SPT]) {
+    if constexpr (sizeof(Real) == 4) {
+        // FP32: the vote and branch cost more than the rescale they would skip
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) acc[u] += rescale<KP>(v[u]);
+        return;
+    }
     Real m[SPT];
     bool low = false;
 #pragma unroll
