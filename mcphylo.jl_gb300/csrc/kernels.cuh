@@ -784,13 +784,12 @@ prune_kernel(const PruneArgs a) {
         }
         if (h[0] >= 0) read_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, NA);
         if (h[1] >= 0) read_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, NB);
-        // the chunk's gradient terms (up to 2 CH rows): lane l sums rows l, l + 32, ..
-        // over the 32 lanes
+        // the chunk's gradient terms: lane l < ng sums row l over the 32 lanes
         int ng = 0;
         auto flush_grad = [&]() {
             __syncwarp();
-            for (int rw = lane; rw < ng; rw += 32) {
-                const Real* row = gbuf + rw * 33;
+            if (lane < ng) {
+                const Real* row = gbuf + lane * 33;
                 Real s0 = Real(0), s1 = Real(0), s2 = Real(0), s3 = Real(0);
 #pragma unroll
                 for (int i = 0; i < 32; i += 4) {
@@ -799,7 +798,7 @@ prune_kernel(const PruneArgs a) {
                     s2 += row[i + 2];
                     s3 += row[i + 3];
                 }
-                pg[gid[rw]] = (s0 + s1) + (s2 + s3);
+                pg[gid[lane]] = (s0 + s1) + (s2 + s3);
             }
             __syncwarp();
             ng = 0;
