@@ -75,16 +75,10 @@ __host__ __device__ constexpr int tip_bytes(int kp, int spt) { return 2 * 32 * s
 __host__ __device__ constexpr int stack_smem_slots(int kp, int spt, int real_bytes) {
     return vec_bytes(kp, spt, real_bytes) <= 1024 ? 6 : vec_bytes(kp, spt, real_bytes) <= 4096 ? 3 : 1;
 }
-// per-lane gradient terms of one chunk (two children per step), reduced once per chunk:
-// 2 CH rows of 33 Reals (padded against bank conflicts) and 2 CH branch indices
-__host__ __device__ constexpr int grad_buf_bytes(int kp, int real_bytes) {
-    return 2 * chunk_steps(kp, real_bytes) * (33 * real_bytes + 4);
-}
 // rounded to 128 bytes so every warp's TMA destinations stay aligned
 __host__ __device__ constexpr int warp_smem_bytes(int kp, int spt, int real_bytes) {
     return (2 * chunk_steps(kp, real_bytes) * (rec_bytes(kp, real_bytes) + tip_bytes(kp, spt)) +
-            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 +
-            grad_buf_bytes(kp, real_bytes) + 127) /
+            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 + 127) /
            128 * 128;
 }
 
@@ -657,8 +651,6 @@ prune_kernel(const PruneArgs a) {
     Real* sstack = reinterpret_cast<Real*>(wbase + 2 * CH * (St::BYTES + St::TIP));
     uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
                                                   NS * SLOT * sizeof(Real));
-    Real* gbuf = reinterpret_cast<Real*>(bars + 2);          // [2 CH][33] gradient terms
-    int* gid = reinterpret_cast<int*>(gbuf + 2 * CH * 33);   // [2 CH] their branches
     St st;
     st.init(wbase, bars, lane, a.wait_limit, a.inject_timeout != 0);
     if (lane == 0) fence_mbar_init();
@@ -784,25 +776,6 @@ prune_kernel(const PruneArgs a) {
         }
         if (h[0] >= 0) read_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, NA);
         if (h[1] >= 0) read_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, NB);
-        // the chunk's gradient terms: lane l < ng sums row l over the 32 lanes
-        int ng = 0;
-        auto flush_grad = [&]() {
-            __syncwarp();
-            if (lane < ng) {
-                const Real* row = gbuf + lane * 33;
-                Real s0 = Real(0), s1 = Real(0), s2 = Real(0), s3 = Real(0);
-#pragma unroll
-                for (int i = 0; i < 32; i += 4) {
-                    s0 += row[i];
-                    s1 += row[i + 1];
-                    s2 += row[i + 2];
-                    s3 += row[i + 3];
-                }
-                pg[gid[lane]] = (s0 + s1) + (s2 + s3);
-            }
-            __syncwarp();
-            ng = 0;
-        };
         for (int j = J - 1; j >= 0; --j) {
             const unsigned char* rj = st.rec(j);
             if (lane == 0) {
@@ -856,10 +829,8 @@ prune_kernel(const PruneArgs a) {
                         }
                         g += valid[u] ? ratio(num, den) : Real(0);
                     }
-                    // reduced across lanes once per chunk (flush_grad)
-                    gbuf[ng * 33 + lane] = g;
-                    if (lane == 0) gid[ng] = h[4 + c];
-                    ++ng;
+                    g = warp_sum(g);
+                    if (lane == 0) pg[h[4 + c]] = g;
                 }
                 if (h[c] >= 0) {
                     Real pbc[SPT][KP];
@@ -871,10 +842,9 @@ prune_kernel(const PruneArgs a) {
                 }
             }
             if (h[1] >= 0) copy_part(pb, Npb);
-            // chunk finished (descending): reduce its gradient terms, refill its buffers
-            // two chunks below
+            // chunk finished (descending): refill its buffers two chunks below
             if (j % CH == 0) {
-                flush_grad();
+                __syncwarp();
                 if (j / CH - 2 >= 0) st.issue(j / CH - 2, lane);
             }
             if (j > 0) {
