@@ -864,18 +864,22 @@ prune_kernel(const PruneArgs a) {
 }
 
 // ---------------------------------------------------------------- step records
-// One thread per (step record, child, rate, row s < Kp): row s of P(t) and dP/dt of
-// the child's branch in FP64, in the reference's order (out2[m,i] = U[m,i] *
-// exp(mu * t * D[i] * rate); P = out2 * Uinv), written transposed (column s of
-// P^T and dP^T) with entry s of the row-sum row; identity for the zero-length
-// virtual branches.  The (c == 0, s == 0) thread also writes the header.
+// R threads per (step record, child, rate) -- R = Kp for Kp >= 8, else 1 -- each
+// taking rows s = s0, s0 + R, .. < Kp: row s of P(t) and dP/dt of the child's branch
+// in FP64, in the reference's order (out2[m,i] = U[m,i] * exp(mu * t * D[i] * rate);
+// P = out2 * Uinv), written transposed (column s of P^T and dP^T) with entry s of the
+// row-sum row; identity for the zero-length virtual branches.  The (c == 0, s0 == 0)
+// thread also writes the header.
+__host__ __device__ constexpr int rec_row_threads(int kp) { return kp >= 8 ? kp : 1; }
+
 template <typename Real>
 __global__ void build_records_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, Kp = a.Kp, C = a.C;
-    if (tid >= int64_t(a.n_steps) * 2 * C * Kp) return;
-    const int s = int(tid % Kp);
-    const int64_t u = tid / Kp;
+    const int R = rec_row_threads(Kp);
+    if (tid >= int64_t(a.n_steps) * 2 * C * R) return;
+    const int s0 = int(tid % R);
+    const int64_t u = tid / R;
     const int r = int(u % C);
     const int c = int((u / C) % 2);
     const int2 sj = a.steps[u / (2 * C)];
@@ -884,7 +888,7 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const SchedNode sn = a.sched[d.sched_off + j];
     const int bytes = rec_bytes(Kp, sizeof(Real));
     unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(bytes);
-    if (c == 0 && s == 0) {
+    if (c == 0 && s0 == 0) {
         int* hd = reinterpret_cast<int*>(rec);
         hd[0] = sn.op[0];
         hd[1] = sn.op[1];
@@ -907,12 +911,14 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     Real* dPT = PT + mat;
     const int b = sn.br[c];
     if (b >= d.n_branch) {
-        for (int k = 0; k < Kp; ++k) {
-            PT[k * Kp + s] = Real(k == s ? 1 : 0);
-            dPT[k * Kp + s] = Real(0);
+        for (int s = s0; s < Kp; s += R) {
+            for (int k = 0; k < Kp; ++k) {
+                PT[k * Kp + s] = Real(k == s ? 1 : 0);
+                dPT[k * Kp + s] = Real(0);
+            }
+            PT[Kp * Kp + s] = Real(s < K ? 1 : 0);
+            dPT[Kp * Kp + s] = Real(0);
         }
-        PT[Kp * Kp + s] = Real(s < K ? 1 : 0);
-        dPT[Kp * Kp + s] = Real(0);
         return;
     }
     const double* U = a.params + d.param_off;
@@ -922,30 +928,32 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const double rate = Uinv[K * K + 1 + r];
     const double t = a.blen[d.blen_off + b];
     double e[32], de[32];
-    if (s < K)
+    if (s0 < K)
         for (int m = 0; m < K; ++m) {
             const double x = exp(mu * t * Dv[m] * rate);
             e[m] = x;
             de[m] = Dv[m] * rate * mu * x;
         }
-    double rs = 0.0, drs = 0.0;
-    for (int k = 0; k < Kp; ++k) {
-        double p = 0.0, dp = 0.0;
-        if (s < K && k < K) {
-            for (int m = 0; m < K; ++m) {
-                p += U[s + K * m] * e[m] * Uinv[m + K * k];
-                dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+    for (int s = s0; s < Kp; s += R) {
+        double rs = 0.0, drs = 0.0;
+        for (int k = 0; k < Kp; ++k) {
+            double p = 0.0, dp = 0.0;
+            if (s < K && k < K) {
+                for (int m = 0; m < K; ++m) {
+                    p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                    dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+                }
+                rs += p;
+                drs += dp;
+            } else {
+                p = (s == k) ? 1.0 : 0.0;
             }
-            rs += p;
-            drs += dp;
-        } else {
-            p = (s == k) ? 1.0 : 0.0;
+            PT[k * Kp + s] = Real(p);
+            dPT[k * Kp + s] = Real(dp);
         }
-        PT[k * Kp + s] = Real(p);
-        dPT[k * Kp + s] = Real(dp);
+        PT[Kp * Kp + s] = Real(rs);
+        dPT[Kp * Kp + s] = Real(drs);
     }
-    PT[Kp * Kp + s] = Real(rs);
-    dPT[Kp * Kp + s] = Real(drs);
 }
 
 // ---------------------------------------------------------------- reduction

@@ -79,7 +79,7 @@ cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStr
 }
 
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st) {
-    const int64_t total = int64_t(a.n_steps) * 2 * a.C * a.Kp;
+    const int64_t total = int64_t(a.n_steps) * 2 * a.C * rec_row_threads(a.Kp);
     if (total == 0) return cudaSuccess;
     const int tpb = 128;
     const int64_t blocks = (total + tpb - 1) / tpb;
