@@ -168,7 +168,7 @@ int mcphy_tc_selftest(int64_t kd, int64_t n, int bf16, const float* a, const flo
  * the handle's own stream. */
 int mcphy_set_stream(mcphy_handle h, void* stream);
 int mcphy_synchronize(mcphy_handle h);
-/* Launch shape of the fused pruning kernel: sites per thread (1, 2, 3 or 4) and
+/* Launch shape of the fused pruning kernel: sites per thread (1, 2 or 4) and
  * threads per block (64..1024, multiple of 32); 0 keeps the automatic choice. */
 int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block);
 /* Picks the fused kernel's launch shape for the current problem: times each

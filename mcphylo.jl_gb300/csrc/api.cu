@@ -113,8 +113,7 @@ void choose_tiles(mcphy_engine* h) {
     if (h->prec == MCPHY_PREC_F64) spt = (h->Kp <= 4) ? std::min(spt, 2) : 1;
     else if (h->Kp == 8) spt = std::min(spt, 2);
     else if (h->Kp > 8) spt = 1;
-    if (spt == 3 && (h->prec == MCPHY_PREC_F64 || h->Kp > 4)) spt = 2;
-    if (spt != 1 && spt != 2 && spt != 3 && spt != 4) spt = 1;
+    if (spt != 1 && spt != 2 && spt != 4) spt = 1;
     h->spt = spt;
     int tpb = h->tpb_req ? h->tpb_req : 128;
     // every warp owns two staging buffers of step records in shared memory
@@ -1057,7 +1056,7 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
         cand = h->Kp <= 4 ? std::vector<std::pair<int, int>>{{1, 128}, {2, 128}, {1, 64}, {2, 64}}
                           : std::vector<std::pair<int, int>>{{1, 128}, {1, 64}};
     else if (h->Kp <= 4)
-        cand = {{4, 128}, {4, 64}, {3, 96}, {3, 64}, {2, 128}, {2, 64}, {4, 256}, {1, 128}};
+        cand = {{4, 128}, {4, 64}, {2, 128}, {2, 64}, {4, 256}, {1, 128}};
     else if (h->Kp <= 8)
         cand = {{1, 128}, {2, 128}, {1, 64}, {2, 64}};
     else

@@ -25,8 +25,8 @@ static const void* fn() { return reinterpret_cast<const void*>(&prune_kernel<KP,
 
 static const void* pick(int Kp, int spt) {
     switch (Kp) {
-        case 2: return spt == 4 ? fn<2, 4>() : spt == 3 ? fn<2, 3>() : spt == 2 ? fn<2, 2>() : fn<2, 1>();
-        case 4: return spt == 4 ? fn<4, 4>() : spt == 3 ? fn<4, 3>() : spt == 2 ? fn<4, 2>() : fn<4, 1>();
+        case 2: return spt == 4 ? fn<2, 4>() : spt == 2 ? fn<2, 2>() : fn<2, 1>();
+        case 4: return spt == 4 ? fn<4, 4>() : spt == 2 ? fn<4, 2>() : fn<4, 1>();
         case 8: return spt == 2 ? fn<8, 2>() : fn<8, 1>();
         case 20: return fn<20, 1>();
         case 32: return fn<32, 1>();
@@ -37,16 +37,8 @@ static const void* pick(int Kp, int spt) {
 cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, const PruneArgs& a,
                              cudaStream_t st) {
     switch (Kp) {
-        case 2:
-            return spt == 4   ? go<2, 4>(blocks, tpb, a, st)
-                   : spt == 3 ? go<2, 3>(blocks, tpb, a, st)
-                   : spt == 2 ? go<2, 2>(blocks, tpb, a, st)
-                              : go<2, 1>(blocks, tpb, a, st);
-        case 4:
-            return spt == 4   ? go<4, 4>(blocks, tpb, a, st)
-                   : spt == 3 ? go<4, 3>(blocks, tpb, a, st)
-                   : spt == 2 ? go<4, 2>(blocks, tpb, a, st)
-                              : go<4, 1>(blocks, tpb, a, st);
+        case 2: return spt == 4 ? go<2, 4>(blocks, tpb, a, st) : spt == 2 ? go<2, 2>(blocks, tpb, a, st) : go<2, 1>(blocks, tpb, a, st);
+        case 4: return spt == 4 ? go<4, 4>(blocks, tpb, a, st) : spt == 2 ? go<4, 2>(blocks, tpb, a, st) : go<4, 1>(blocks, tpb, a, st);
         case 8: return spt == 2 ? go<8, 2>(blocks, tpb, a, st) : go<8, 1>(blocks, tpb, a, st);
         case 20: return go<20, 1>(blocks, tpb, a, st);
         case 32: return go<32, 1>(blocks, tpb, a, st);
