@@ -398,27 +398,6 @@ def run_nuts(args):
 
 
 # ----------------------------------------------------------------------------- GPU arm
-def autotune(insts, steps=2):
-    """Sites per thread x threads per block of the fused kernel, best device time."""
-    K = insts[0].K
-    cands = [(1, 256), (2, 256), (2, 128), (4, 128), (1, 128), (4, 256)] if K <= 4 else \
-        [(1, 256), (2, 128), (1, 128)] if K <= 8 else [(1, 128), (1, 64)]
-    res = {}
-    for spt, tpb in cands:
-        e = make_engine(insts, "f32", (spt, tpb))
-        e.enable_timing(True)
-        e.logpdf_grad()
-        ts = []
-        for _ in range(steps):
-            e.logpdf_grad()
-            ts.append(e.timing()["prune_ms"])
-        res[f"{spt}x{tpb}"] = min(ts)
-        e.close()
-    best = min(res, key=res.get)
-    spt, tpb = (int(x) for x in best.split("x"))
-    return (spt, tpb), res
-
-
 def run_gpu(args, rank, world):
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
