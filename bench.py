@@ -50,8 +50,9 @@ def make_workload(name, workers):
                "sites": "logU[500,50000]", "model": "HKY+G4 (shape 0.5), kappa~LogNormal(1,0.5)",
                "states": 4, "rates": 4}
     elif name == "gtr-g4":
-        insts = [simulate.gtr_gamma(S=100_000, with_weights=False)]
-        cfg = {"workload": "gtr-g4", "taxa": 128, "sites": 100_000, "model": "GTR+G4 (shape 0.5)",
+        insts = [simulate.gtr_gamma(S=100_000, with_weights=True)]
+        cfg = {"workload": "gtr-g4", "taxa": 128, "sites": "100,000 patterns",
+               "pattern_weights": "Poisson(1)+1", "model": "GTR+G4 (shape 0.5)",
                "states": 4, "rates": 4}
     elif name == "restriction":
         insts = [simulate.restriction_small()]
@@ -79,6 +80,8 @@ def make_engine(insts, precision, tiles=None):
     for i, b in enumerate(insts):
         e.set_tree(b.parent, b.blen, i)
         e.set_codes(b.codes, b.leaf_nums, i)
+        if b.weights is not None:
+            e.set_weights(b.weights, i)
         e.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, i)
     return e
 

@@ -113,6 +113,14 @@ int mcphy_batch_set_data(mcphy_handle h, int64_t i, const double* x, int64_t nsi
  * (bit k = state k allowed) of leaf leaf_nums[l] at site s. */
 int mcphy_batch_set_codes(mcphy_handle h, int64_t i, const uint32_t* codes, int64_t nsites,
                           const int64_t* leaf_nums, int64_t n_leaves);
+/* Site-pattern weights (no counterpart in the reference, whose sites all count
+ * once): weights[s] >= 0 multiplies site s's log-likelihood and gradient terms, so a
+ * column that occurs w times can be sent once with weight w.  nsites must equal the
+ * instance's sites; NULL restores unit weights.  Setting new data with a different
+ * number of sites clears them. */
+int mcphy_batch_set_weights(mcphy_handle h, int64_t i, const double* weights, int64_t nsites);
+int mcphy_set_weights(mcphy_handle h, const double* weights, int64_t nsites);
+
 int mcphy_batch_set_tree(mcphy_handle h, int64_t i, int64_t nnodes, const int64_t* parent,
                          const double* blen);
 int mcphy_batch_set_branch_lengths(mcphy_handle h, int64_t i, const double* blen);

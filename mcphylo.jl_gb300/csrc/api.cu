@@ -152,7 +152,7 @@ int layout(mcphy_engine* h) {
     int64_t sched_off = 0, rec_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
             pgrad_off = 0, blen_off = 0, nsteps = 0;
     const int64_t psize = param_size(K, Kp, C);
-    int64_t lc_off = 0;
+    int64_t lc_off = 0, w_off = 0;
     h->lc_off.assign(h->M, 0);
     for (int64_t i = 0; i < h->M; ++i) {
         Inst& in = h->inst[i];
@@ -204,6 +204,8 @@ int layout(mcphy_engine* h) {
         h->lc_off[i] = lc_off;
         d.lcode_off = lc_off;
         if (!in.dense) lc_off += int64_t(d.n_leaf) * d.S_pad;
+        d.weight_off = w_off;
+        w_off += d.S_pad;
         param_off += psize;
         const int64_t items = int64_t(C) * d.n_blocks;
         item_off += items;
@@ -223,6 +225,7 @@ int layout(mcphy_engine* h) {
     h->rec_bytes_total = rec_off;
     h->leaf_elems = leaf_off;
     h->leafcode_elems = lc_off;
+    h->weight_elems = w_off;
     if (h->n_items >= (int64_t(1) << 31)) return fail(h, MCPHY_ERR_ARG, "too many work items");
 
     // work items and the order warps take them: largest trees first
@@ -270,6 +273,7 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_codes, code_bytes * size_t(h->leaf_elems)))) return rc;
     if ((rc = ensure(h, h->d_leafcodes, code_bytes * size_t(std::max<int64_t>(h->leafcode_elems, 64)))))
         return rc;
+    if ((rc = ensure(h, h->d_weights, sizeof(double) * size_t(h->weight_elems)))) return rc;
     if ((rc = ensure(h, h->d_dense, h->any_dense ? rs * size_t(h->leaf_elems) : 256))) return rc;
     if ((rc = ensure_pinned(h, h->h_blen, h->h_blen_cap, size_t(h->total_branch)))) return rc;
     if ((rc = ensure_pinned(h, h->h_out, h->h_out_cap, size_t(h->M + h->total_branch) + 1))) return rc;
@@ -392,6 +396,14 @@ int upload_data(mcphy_engine* h) {
         if (f64) CK(cudaMemcpy(h->d_dense.p, dd.data(), dd.size() * 8, cudaMemcpyHostToDevice));
         else CK(cudaMemcpy(h->d_dense.p, df.data(), df.size() * 4, cudaMemcpyHostToDevice));
     }
+    // site-pattern weights: the caller's, or 1 per site; 0 on padding sites
+    std::vector<double> w(size_t(h->weight_elems), 0.0);
+    for (int64_t i = 0; i < h->M; ++i) {
+        const Inst& in = h->inst[i];
+        double* wi = w.data() + h->desc[i].weight_off;
+        for (int64_t s = 0; s < in.S; ++s) wi[s] = in.weights.empty() ? 1.0 : in.weights[s];
+    }
+    CK(cudaMemcpy(h->d_weights.p, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_desc.p, h->desc.data(), sizeof(InstanceDesc) * h->M, cudaMemcpyHostToDevice));
     // leaf codes in schedule order: entry (block, step j, operand c) holds the codes of
     // the block's sites for the leaf that is operand c of step j
@@ -544,6 +556,7 @@ int run(mcphy_engine* h, bool want_grad) {
     a.inject_timeout = h->inject == 1 ? 1 : 0;
     a.lcodes = h->d_leafcodes.p;
     a.sched = static_cast<const SchedNode*>(h->d_sched.p);
+    a.weights = static_cast<const double*>(h->d_weights.p);
     h->inject = 0;
     CK(tc    ? launch_prune_tc(fmt, h->K, h->blocks, a, st)
        : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
@@ -665,6 +678,7 @@ int set_data_common(mcphy_engine* h, int64_t i, int64_t nsites, int64_t nnodes,
     const bool reshaped = (in.S != nsites) || (in.data_N != nnodes) ||
                           (int64_t(in.leaf_nums.size()) != n_leaves) ||
                           !std::equal(in.leaf_nums.begin(), in.leaf_nums.end(), leaf_nums);
+    if (in.S != nsites) in.weights.clear();   // weights belong to an alignment of S sites
     in.S = nsites;
     in.data_N = nnodes;
     in.leaf_nums.assign(leaf_nums, leaf_nums + n_leaves);
@@ -839,6 +853,30 @@ int mcphy_batch_set_codes(mcphy_handle h, int64_t i, const uint32_t* codes, int6
     in.dvals.clear();
     in.codes.assign(codes, codes + n_leaves * nsites);
     return MCPHY_OK;
+}
+
+int mcphy_batch_set_weights(mcphy_handle h, int64_t i, const double* weights, int64_t nsites) {
+    int rc;
+    if ((rc = check_instance(h, i))) return rc;
+    Inst& in = h->inst[i];
+    if (!in.has_data) return fail(h, MCPHY_ERR_STATE, "set the data before the weights");
+    if (!weights) {
+        in.weights.clear();
+    } else {
+        if (nsites != in.S)
+            return fail(h, MCPHY_ERR_SHAPE, "weights: " + std::to_string(nsites) + " entries for " +
+                                                std::to_string(in.S) + " sites");
+        for (int64_t s = 0; s < nsites; ++s)
+            if (!std::isfinite(weights[s]) || weights[s] < 0.0)
+                return fail(h, MCPHY_ERR_DATA, "weights must be finite and non-negative");
+        in.weights.assign(weights, weights + nsites);
+    }
+    h->dirty |= DIRTY_DATA;
+    return MCPHY_OK;
+}
+
+int mcphy_set_weights(mcphy_handle h, const double* weights, int64_t nsites) {
+    return mcphy_batch_set_weights(h, 0, weights, nsites);
 }
 
 int mcphy_batch_set_tree(mcphy_handle h, int64_t i, int64_t nnodes, const int64_t* parent,

@@ -31,6 +31,7 @@ struct Inst {
     bool dense = false;
     std::vector<uint32_t> codes;   // [leaf_row][S]
     std::vector<double> dvals;     // [leaf_row][S][K]
+    std::vector<double> weights;   // [S] site-pattern weights; empty = every site once
     bool has_data = false;
     // model
     std::vector<double> U, D, Uinv, pi, rates;
@@ -74,12 +75,13 @@ struct mcphy_engine {
     int32_t max_pre = 0;
     int64_t leaf_elems = 0;
     int64_t leafcode_elems = 0;       // leaf-major code copy (code units)
+    int64_t weight_elems = 0;         // site-pattern weights (doubles)
     std::vector<int64_t> lc_off;      // per instance, into d_leafcodes
     bool any_dense = false;
     std::vector<SchedNode> sched_all;
 
     DevBuf d_desc, d_sched, d_items, d_queue, d_steps, d_recs, d_codes, d_dense, d_params,
-        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter, d_leafcodes;
+        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter, d_leafcodes, d_weights;
     int n_split = 1;
 
     double* h_blen = nullptr;

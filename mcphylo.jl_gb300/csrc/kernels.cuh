@@ -106,6 +106,7 @@ struct PruneArgs {
     int32_t inject_timeout;   // test hook: never issue the first staging copy
     const void* lcodes;       // leaf-major state codes [row][S_pad] (tensor-core path)
     const SchedNode* sched;   // schedule nodes (tensor-core path: sweep prologues)
+    const double* weights;    // site-pattern weights per instance [S_pad], 0 past S
 };
 
 // ---------------------------------------------------------------- tensor-core records
@@ -678,8 +679,12 @@ prune_kernel(const PruneArgs a) {
         const Real* dense = reinterpret_cast<const Real*>(a.dense) + d.leaf_off;
 
         bool valid[SPT];
+        double wt[SPT];            // site-pattern weight (each site's log and gradient terms)
 #pragma unroll
-        for (int u = 0; u < SPT; ++u) valid[u] = (site0 + 32 * u) < d.S;
+        for (int u = 0; u < SPT; ++u) {
+            valid[u] = (site0 + 32 * u) < d.S;
+            wt[u] = __ldg(a.weights + d.weight_off + site0 + 32 * u);
+        }
 
         // operand c of step j when it is a leaf, into L
         auto leaf = [&](int j, int c, int op, Real (&L)[SPT][KP]) {
@@ -740,7 +745,7 @@ prune_kernel(const PruneArgs a) {
                     for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Da[u][k], lik);
                     const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
                     const double v = log_site(lik) + double(ex) * LN2;
-                    ll_lane += valid[u] ? v : 0.0;
+                    ll_lane += valid[u] ? wt[u] * v : 0.0;
                 }
             }
             // chunk finished: refill its buffers with the chunk after next
@@ -827,7 +832,7 @@ prune_kernel(const PruneArgs a) {
                             num = fma(pt[u][k], dD[u][k], num);
                             den = fma(pt[u][k], D[c][u][k], den);
                         }
-                        g += valid[u] ? ratio(num, den) : Real(0);
+                        g += valid[u] ? Real(wt[u]) * ratio(num, den) : Real(0);
                     }
                     g = warp_sum(g);
                     if (lane == 0) pg[h[4 + c]] = g;

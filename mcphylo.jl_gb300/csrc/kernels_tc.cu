@@ -384,6 +384,8 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         const int blk = it.y - r * d.n_blocks;
         const int site = blk * TC_M + t;
         const bool valid = site < d.S;
+        const double wt = __ldg(a.weights + d.weight_off + site);   // site-pattern weight
+        const float wtf = float(wt);
         const int J = d.J;
         const unsigned char* recs = a.recs + d.rec_off + size_t(r) * size_t(J) * size_t(RB);
         const uint32_t* lc = reinterpret_cast<const uint32_t*>(a.lcodes) + d.lcode_off + site;
@@ -454,7 +456,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 for (int k = 0; k < KD; ++k)
                     if (k < K) lik = fmaf(float(__ldg(pi_d + k)), D0[k], lik);
                 const int ex = int(eacc) - J * 127;
-                ll += valid ? log(double(lik)) + double(ex) * LN2 : 0.0;
+                ll += valid ? wt * (log(double(lik)) + double(ex) * LN2) : 0.0;
             }
             code0 = ncode0;
             code1 = ncode1;
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D0[k];
                 float num, den;
                 dot2<VK>(pt, dD, D1, num, den);
-                g1 = valid ? __fdividef(num, den) : 0.f;
+                g1 = valid ? wtf * __fdividef(num, den) : 0.f;
                 if (op1 >= 0) write_a<VK, FMT>(tile(b, 1), t, pt);
             }
             {
@@ -588,7 +590,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D1[k];
                 float num, den;
                 dot2<VK>(pt, dD, D0, num, den);
-                g0 = valid ? __fdividef(num, den) : 0.f;
+                g0 = valid ? wtf * __fdividef(num, den) : 0.f;
                 if (op0 >= 0) write_a<VK, FMT>(tile(b, 0), t, pt);
             }
             g0 = warp_sum(g0);

@@ -57,6 +57,7 @@ struct alignas(16) InstanceDesc {
     int64_t blen_off;    // into the packed branch-length vector
     int64_t grad_off;    // into the packed gradient output
     int64_t lcode_off;   // into the leaf-major code copy [row][S_pad] (code units)
+    int64_t weight_off;  // into the site-pattern weights (S_pad doubles, 0 past S)
 };
 
 // FP64 model parameters of one instance, packed at param_off:

@@ -196,6 +196,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     a.C = h->C;
     a.want_grad = 1;
     a.wait_limit = kWaitLimit;
+    a.weights = static_cast<const double*>(h->d_weights.p);
     a.inject_timeout = 0;
     NA_CK(f64 ? launch_prune_f64(h->Kp, h->spt, int(blocks), h->tpb, a, st)
               : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, a, st));

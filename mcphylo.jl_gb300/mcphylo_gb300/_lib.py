@@ -55,6 +55,8 @@ SIGNATURES = {
     "mcphy_logpdf_device": (c_int, [handle_t, ctypes.c_void_p]),
     "mcphy_logpdf_grad_noalloc": (c_int, [handle_t, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "mcphy_batch_set_weights": (c_int, [handle_t, i64, pdbl, i64]),
+    "mcphy_set_weights": (c_int, [handle_t, pdbl, i64]),
     "mcphy_tc_selftest": (c_int, [ctypes.c_int64, ctypes.c_int64, c_int, P(ctypes.c_float),
                                   P(ctypes.c_float), P(ctypes.c_float)]),
     "mcphy_set_stream": (c_int, [handle_t, ctypes.c_void_p]),

@@ -87,6 +87,14 @@ class Engine:
         check(self._L.mcphy_batch_set_codes(self._h, i, c.ctypes.data_as(_lib.pu32), c.shape[1],
                                             _pi64(ln), len(ln)), self._h, "set_codes")
 
+    def set_weights(self, weights: Optional[Sequence[float]], i: int = 0) -> None:
+        """Site-pattern weights (one per site of instance i; None: every site once)."""
+        if weights is None:
+            check(self._L.mcphy_batch_set_weights(self._h, i, None, 0), self._h, "set_weights")
+            return
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        check(self._L.mcphy_batch_set_weights(self._h, i, _pd(w), len(w)), self._h, "set_weights")
+
     def set_tree(self, parent: Sequence[int], blen: Optional[Sequence[float]] = None,
                  i: int = 0) -> None:
         p = np.ascontiguousarray(parent, dtype=np.int64)

@@ -121,3 +121,22 @@ def codes_from_tensor(x: np.ndarray, leaf_nums) -> Tuple[np.ndarray, bool]:
         return None, False
     w = (1 << np.arange(K, dtype=np.uint64))[None, :, None]
     return (sl.astype(np.uint64) * w).sum(axis=1).astype(np.uint32), True
+
+
+def compress_patterns(codes: np.ndarray) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Site-pattern compression of an (n_leaves, S) code matrix: the distinct
+    columns, in order of first appearance, how often each occurs (the weights
+    Engine.set_weights takes) and, for every original site, its pattern's index.
+    logL and the gradient over the weighted patterns equal those over all sites.
+    (The reference evaluates every column; this is an input-side saving.)"""
+    c = np.ascontiguousarray(np.asarray(codes).T)
+    if c.shape[0] == 0:
+        return np.asarray(codes)[:, :0], np.zeros(0), np.zeros(0, dtype=np.int64)
+    view = c.view(np.dtype((np.void, c.dtype.itemsize * c.shape[1])))[:, 0]
+    _, first, inverse, counts = np.unique(view, return_index=True, return_inverse=True,
+                                          return_counts=True)
+    order = np.argsort(first, kind="stable")          # patterns by first appearance
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    patterns = np.asarray(codes)[:, first[order]]
+    return patterns, counts[order].astype(np.float64), rank[inverse.ravel()].astype(np.int64)

@@ -380,3 +380,93 @@ def test_autotune_keeps_results(built_lib):
     ll1, g1 = e.logpdf_grad()
     assert abs(ll1 - ll0) <= 1e-9 * abs(ll0)
     assert_grad_close(g1, g0, 1e-5, F32_G_FLOOR)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "tf32"])
+def test_site_pattern_weights(built_lib, precision):
+    """A pattern of weight w counts as w identical columns: the weighted evaluation
+    equals the oracle on the column-expanded alignment."""
+    K = 20 if precision == "tf32" else 4
+    inst = random_instance(K, 2, 18, 130, seed=71)
+    w = np.random.default_rng(5).poisson(1.0, inst.S) + 1
+    expanded = simulate.Instance(inst.tree, inst.parent, inst.blen, inst.leaf_nums,
+                                 np.repeat(inst.codes, w, axis=1), inst.U, inst.D, inst.Uinv,
+                                 inst.mu, inst.pi, inst.rates)
+    llo, go = oracle(expanded)
+    e = mp.Engine(K, 2, precision)
+    e.set_tree(inst.parent, inst.blen)
+    e.set_codes(inst.codes, inst.leaf_nums)
+    e.set_weights(w.astype(float))
+    e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    ll, g = e.logpdf_grad()
+    if precision == "f64":
+        assert abs(ll - llo) <= F64_RTOL * abs(llo)
+        assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
+    elif precision == "f32":
+        assert abs(ll - llo) <= F32_LL_RTOL * abs(llo)
+        assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
+    else:
+        assert abs(ll - llo) <= 5e-4 * abs(llo)
+        assert np.max(np.abs(g - go)) <= 5e-3 * np.max(np.abs(go))
+    # unit weights again: the plain alignment
+    e.set_weights(None)
+    llu, _ = e.logpdf_grad()
+    llp, _ = oracle(inst)
+    tol = F64_RTOL if precision == "f64" else 5e-4
+    assert abs(llu - llp) <= tol * abs(llp)
+
+
+def test_compressed_patterns_match_full_alignment(built_lib):
+    """Site-pattern compression: the distinct columns with their counts give the
+    same logL and gradient as every column."""
+    inst = random_instance(2, 4, 25, 3000, seed=72, model="restriction", missing=0.0)
+    pat, w, idx = parse.compress_patterns(inst.codes)
+    assert pat.shape[1] < inst.S and np.array_equal(pat[:, idx], inst.codes)
+    full = engine(inst, "f64")
+    llf, gf = full.logpdf_grad()
+    e = mp.Engine(2, 4, "f64")
+    e.set_tree(inst.parent, inst.blen)
+    e.set_codes(pat, inst.leaf_nums)
+    e.set_weights(w)
+    e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    ll, g = e.logpdf_grad()
+    assert abs(ll - llf) <= 1e-12 * abs(llf)
+    assert_grad_close(g, gf, F64_G_RTOL, F64_G_FLOOR)
+
+
+def test_weights_are_checked(built_lib):
+    inst = random_instance(4, 1, 8, 40, seed=73)
+    e = mp.Engine(4, 1, "f64")
+    e.set_tree(inst.parent, inst.blen)
+    with pytest.raises(mp.MCPhyError):
+        e.set_weights(np.ones(40))                 # no data yet
+    e.set_codes(inst.codes, inst.leaf_nums)
+    with pytest.raises(mp.DimensionMismatch):
+        e.set_weights(np.ones(39))
+    with pytest.raises(ValueError):
+        e.set_weights(-np.ones(40))
+
+
+def test_gradient_vs_central_fd_at_scale(built_lib):
+    """Branch-length gradient at scale (restriction+G4, 512-taxon birth-death tree,
+    20,000 sites): the FP64 adjoint against central finite differences
+    (h = 1e-6) on a sample of branches, and the FP32 gradient against it."""
+    inst = simulate.restriction_gamma_bd()
+    e = engine(inst, "f64")
+    ll, g = e.logpdf_grad()
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    for i in rng.choice(inst.N - 1, 12, replace=False):
+        b = inst.blen.copy()
+        b[i] += h
+        e.set_branch_lengths(b)
+        lp = e.logpdf()
+        b[i] -= 2 * h
+        e.set_branch_lengths(b)
+        lm = e.logpdf()
+        fd = (lp - lm) / (2 * h)
+        # FP64 noise of a 1e5-magnitude logL over 2h is ~1e-4 in the difference quotient
+        assert abs(fd - g[i]) <= 1e-4 * max(1.0, abs(g[i])), (i, fd, g[i])
+    ll32, g32 = engine(inst, "f32").logpdf_grad()
+    assert abs(ll32 - ll) <= F32_LL_RTOL * abs(ll)
+    assert_grad_close(g32, g, F32_G_RTOL, F32_G_FLOOR)

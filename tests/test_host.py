@@ -218,3 +218,13 @@ def test_simulators_make_valid_instances(built_lib):
     assert mp.schedule_info(bd.parent)["leaves"] == 40
     batch = mp.simulate.hky_batch(n=3, scale=0.01)
     assert len(batch) == 3 and all(b.K == 4 and len(b.rates) == 4 for b in batch)
+
+
+def test_compress_patterns():
+    from mcphylo_gb300.parse import compress_patterns
+    codes = np.array([[1, 2, 1, 1, 2], [2, 2, 2, 1, 2]], dtype=np.uint32)
+    pat, w, idx = compress_patterns(codes)
+    np.testing.assert_array_equal(pat, [[1, 2, 1], [2, 2, 1]])
+    np.testing.assert_array_equal(w, [2, 2, 1])
+    np.testing.assert_array_equal(idx, [0, 1, 0, 2, 1])
+    np.testing.assert_array_equal(pat[:, idx], codes)
