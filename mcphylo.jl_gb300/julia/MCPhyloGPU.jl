@@ -132,4 +132,33 @@ function gradlogpdf(d::GPUPhyloDist, x::AbstractArray)
     ll[], grad
 end
 
+# ------------------------------------------------------------------ reverse mode
+# `loglik(gpd, blen)`: the log-likelihood as a function of the branch-length vector
+# (num order), with a ChainRules rrule whose pullback is the engine's adjoint
+# gradient, so Zygote (which MCPhylo uses) differentiates through it.
+import ChainRulesCore
+
+function loglik(d::GPUPhyloDist, blen::AbstractVector{<:Real})
+    check(ccall((:mcphy_set_branch_lengths, libmcphy), Cint, (Ptr{Cvoid}, Ptr{Float64}),
+                d.h.ptr, Vector{Float64}(blen)), d.h.ptr)
+    d.blen = Vector{Float64}(blen)
+    ll = Ref{Float64}(0.0)
+    check(ccall((:mcphy_logpdf, libmcphy), Cint, (Ptr{Cvoid}, Ref{Float64}), d.h.ptr, ll), d.h.ptr)
+    ll[]
+end
+
+function ChainRulesCore.rrule(::typeof(loglik), d::GPUPhyloDist, blen::AbstractVector{<:Real})
+    check(ccall((:mcphy_set_branch_lengths, libmcphy), Cint, (Ptr{Cvoid}, Ptr{Float64}),
+                d.h.ptr, Vector{Float64}(blen)), d.h.ptr)
+    d.blen = Vector{Float64}(blen)
+    ll = Ref{Float64}(0.0)
+    grad = Vector{Float64}(undef, length(blen))
+    check(ccall((:mcphy_logpdf_grad, libmcphy), Cint, (Ptr{Cvoid}, Ref{Float64}, Ptr{Float64}),
+                d.h.ptr, ll, grad), d.h.ptr)
+    pullback(Δ) = (ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), Δ .* grad)
+    return ll[], pullback
+end
+
+export loglik
+
 end # module
