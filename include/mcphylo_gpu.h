@@ -196,10 +196,12 @@ int mcphy_get_timing(mcphy_handle h, float* ms3);
  * (sum over instances of (N_i-1)*S_i*C), [2] bytes of device scratch in use. */
 int mcphy_get_counts(mcphy_handle h, int64_t* counts3);
 const char* mcphy_last_error(mcphy_handle h);
-/* Test hook, no counterpart in the reference: kind 1 makes the next evaluation's
+/* Test hook, no counterpart in the reference.  kind 1 makes the next evaluation's
  * first staging wait run out (its copy is never issued) so that the bounded-wait
  * path can be tested without a device fault; that evaluation returns
- * MCPHY_ERR_TIMEOUT and later ones are unaffected.  kind 0 clears it. */
+ * MCPHY_ERR_TIMEOUT and later ones are unaffected.  kind 2 makes the next device
+ * allocation fail (MCPHY_ERR_OOM); the handle keeps its state and the next call
+ * retries.  kind 0 clears either. */
 int mcphy_debug_inject(mcphy_handle h, int kind);
 const char* mcphy_status_string(int status);
 /* Library version as major*10000 + minor*100 + patch. */

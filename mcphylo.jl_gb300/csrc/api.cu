@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine_state.h"
 #include "kernels.cuh"
 #include "mcphy_internal.h"
@@ -20,6 +22,14 @@
 using namespace mcphy;
 
 namespace {
+
+// NVTX range for profilers (no cost without a tool attached)
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 
 int kp_of(int K) {
     if (K <= 2) return 2;
@@ -56,6 +66,10 @@ int fail(mcphy_engine* h, int code, const std::string& msg) {
 int ensure(mcphy_engine* h, DevBuf& b, size_t bytes) {
     if (bytes == 0) bytes = 256;
     if (b.cap >= bytes) return MCPHY_OK;
+    if (h->inject == 2) {   // test hook: this allocation fails
+        h->inject = 0;
+        return fail(h, MCPHY_ERR_OOM, "device allocation failed (injected by mcphy_debug_inject)");
+    }
     if (b.p) {
         cudaFree(b.p);
         b.p = nullptr;
@@ -133,6 +147,7 @@ void drop_graphs(mcphy_engine* h) {
 
 // Rebuilds schedules, offsets, work items and device tables.
 int layout(mcphy_engine* h) {
+    Range nv("mcphy_layout");
     drop_graphs(h);
     choose_tiles(h);
     const int SB = 32 * h->spt;
@@ -419,6 +434,7 @@ int upload_data(mcphy_engine* h) {
 // captured graphs stay valid; a schedule whose step count or stack depth no
 // longer fits the layout falls back to a full layout.
 int retopo(mcphy_engine* h) {
+    Range nv("mcphy_topology");
     std::vector<std::pair<int64_t, Schedule>> todo;
     for (int64_t i = 0; i < h->M; ++i) {
         Inst& in = h->inst[i];
@@ -552,12 +568,12 @@ int run(mcphy_engine* h, bool want_grad) {
     a.K = h->K;
     a.C = h->C;
     a.want_grad = want_grad ? 1 : 0;
-    a.wait_limit = h->inject ? 4096 : kWaitLimit;
+    a.wait_limit = h->inject == 1 ? 4096 : kWaitLimit;
     a.inject_timeout = h->inject == 1 ? 1 : 0;
     a.lcodes = h->d_leafcodes.p;
     a.sched = static_cast<const SchedNode*>(h->d_sched.p);
     a.weights = static_cast<const double*>(h->d_weights.p);
-    h->inject = 0;
+    if (h->inject == 1) h->inject = 0;
     CK(tc    ? launch_prune_tc(fmt, h->K, h->blocks, a, st)
        : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
              : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
@@ -636,6 +652,7 @@ int graph_for(mcphy_engine* h, bool want_grad, cudaGraphExec_t* out) {
 }
 
 int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
+    Range nv(want_grad ? "mcphy_logpdf_grad" : "mcphy_logpdf");
     if (!h) return MCPHY_ERR_ARG;
     if (!ll) return fail(h, MCPHY_ERR_ARG, "ll is NULL");
     if (want_grad && !grad) return fail(h, MCPHY_ERR_ARG, "grad is NULL");
@@ -643,7 +660,7 @@ int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
     if ((rc = prepare(h))) return rc;
     int32_t* flag = reinterpret_cast<int32_t*>(h->h_out + h->M + h->total_branch);
     *flag = 0;
-    if (h->use_graph && !h->timing && !h->inject) {
+    if (h->use_graph && !h->timing && h->inject != 1) {
         cudaGraphExec_t ex = nullptr;
         if ((rc = graph_for(h, want_grad, &ex))) return rc;
         CK(cudaGraphLaunch(ex, h->stream));
@@ -1007,6 +1024,7 @@ int mcphy_set_all_branch_lengths_device(mcphy_handle h, const double* d_blen_pac
 }
 
 int mcphy_logpdf_grad_device(mcphy_handle h, double* d_ll, double* d_grad_packed) {
+    Range nv("mcphy_logpdf_grad_device");
     if (!h) return MCPHY_ERR_ARG;
     if (!d_ll || !d_grad_packed) return fail(h, MCPHY_ERR_ARG, "NULL output");
     int rc;
@@ -1020,6 +1038,7 @@ int mcphy_logpdf_grad_device(mcphy_handle h, double* d_ll, double* d_grad_packed
 }
 
 int mcphy_logpdf_device(mcphy_handle h, double* d_ll) {
+    Range nv("mcphy_logpdf_device");
     if (!h) return MCPHY_ERR_ARG;
     if (!d_ll) return fail(h, MCPHY_ERR_ARG, "NULL output");
     int rc;
@@ -1065,7 +1084,7 @@ int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block)
 
 int mcphy_debug_inject(mcphy_handle h, int kind) {
     if (!h) return MCPHY_ERR_ARG;
-    if (kind != 0 && kind != 1) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
+    if (kind < 0 || kind > 2) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
     h->inject = kind;
     return MCPHY_OK;
 }

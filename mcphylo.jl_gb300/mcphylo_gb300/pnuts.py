@@ -398,6 +398,33 @@ class PNUTS:
         self.n_grad_evals = 0
         self.n_logf_evals = 0
 
+    # -- checkpoint / resume (the sampler state a Chains file carries in the
+    #    reference, output/fileio.jl:15-35 and model/mcmc.jl:17-58)
+    _STATE = ("parent", "blen", "tree_depth", "delta", "jitter_amt", "epsilon", "m", "s_bar",
+              "x_bar", "mu_p", "delta_p", "gamma_p", "kappa_p", "t0_p", "delta_nni",
+              "metro_acc_prob", "nni_stat", "adapt", "moves", "att_moves", "tree_depth_trace",
+              "acc_p_r", "lf", "n_grad_evals", "n_logf_evals", "max_refractions")
+
+    def state(self) -> dict:
+        """Everything needed to continue the chain: tree, step-size adapter, traces
+        and the random generator's state (a picklable dict)."""
+        out = {k: (v.copy() if isinstance(v, (np.ndarray, list)) else v)
+               for k, v in ((k, getattr(self, k)) for k in self._STATE)}
+        out["rng"] = self.rng.bit_generator.state
+        out["rng_kind"] = type(self.rng.bit_generator).__name__
+        return out
+
+    @classmethod
+    def from_state(cls, state: dict, logfgrad: Callable, logf: Callable) -> "PNUTS":
+        """A sampler that continues exactly where the one `state` came from."""
+        bg = getattr(np.random, state["rng_kind"])()
+        bg.state = state["rng"]
+        s = cls(state["parent"], state["blen"], logfgrad, logf, rng=np.random.Generator(bg))
+        for k in cls._STATE:
+            v = state[k]
+            setattr(s, k, v.copy() if isinstance(v, (np.ndarray, list)) else v)
+        return s
+
     # -- evaluation counting
     def _fg(self, parent, blen):
         self.n_grad_evals += 1

@@ -470,3 +470,23 @@ def test_gradient_vs_central_fd_at_scale(built_lib):
     ll32, g32 = engine(inst, "f32").logpdf_grad()
     assert abs(ll32 - ll) <= F32_LL_RTOL * abs(ll)
     assert_grad_close(g32, g, F32_G_RTOL, F32_G_FLOOR)
+
+
+def test_injected_allocation_failure_is_reported_and_recoverable(built_lib):
+    """mcphy_debug_inject(2): the next device allocation fails with MCPHY_ERR_OOM;
+    the handle keeps its state and the next call succeeds with the same result."""
+    inst = random_instance(4, 2, 30, 300, seed=91)
+    e = engine(inst, "f32")
+    ll0, g0 = e.logpdf_grad()
+    bigger = random_instance(4, 2, 60, 900, seed=92)   # needs larger buffers
+    e.set_tree(bigger.parent, bigger.blen)
+    e.set_codes(bigger.codes, bigger.leaf_nums)
+    e.set_model(bigger.U, bigger.D, bigger.Uinv, bigger.mu, bigger.pi, bigger.rates)
+    e.debug_inject(2)
+    with pytest.raises(mp.MCPhyError) as ei:
+        e.logpdf_grad()
+    assert ei.value.status == -4
+    ll1, g1 = e.logpdf_grad()
+    llo, go = oracle(bigger)
+    assert abs(ll1 - llo) <= F32_LL_RTOL * abs(llo)
+    assert_grad_close(g1, go, F32_G_RTOL, F32_G_FLOOR)

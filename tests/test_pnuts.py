@@ -307,3 +307,26 @@ def test_chain_with_oracle_likelihood():
     ch = P.run_chain(inst.parent, inst.blen, lfg, lf, n_iter=15, n_adapt=10, seed=2, target=0.8)
     assert np.all(np.isfinite(ch.logf)) and np.all(ch.blen > 0)
     assert ch.grad_evals >= 15
+
+
+def test_checkpoint_resume_continues_the_chain():
+    """state() / from_state(): a restored sampler draws exactly what the original
+    would have drawn (tree, step size, adapter and random stream)."""
+    import pickle
+    tree = yule_tree(8, np.random.default_rng(0), 0.1)
+    parent, blen = to_parent(tree)
+    lf = lambda p, b: _gamma_target(p, b)[0]
+    a = P.PNUTS(parent, np.full(len(blen), 1.0), _gamma_target, lf,
+                rng=np.random.default_rng(11), target=0.8)
+    for it in range(15):
+        a.sample(it < 10)
+    saved = pickle.loads(pickle.dumps(a.state()))
+    for _ in range(6):
+        a.sample(False)
+    b = P.PNUTS.from_state(saved, _gamma_target, lf)
+    for _ in range(6):
+        b.sample(False)
+    np.testing.assert_array_equal(a.parent, b.parent)
+    np.testing.assert_array_equal(a.blen, b.blen)
+    assert a.epsilon == b.epsilon and a.tree_depth_trace == b.tree_depth_trace
+    assert a.n_grad_evals == b.n_grad_evals
