@@ -500,6 +500,23 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Packed two-lane FP32 arithmetic (fma.rn.f32x2 / mul.rn.f32x2): each lane is the
+// same correctly rounded operation as the scalar form, so pairing independent
+// operations halves the instructions and changes no result.
+__device__ __forceinline__ void fma2(float a0, float a1, float b0, float b1, float& c0, float& c1) {
+    const float2 r = __ffma2_rn(make_float2(a0, a1), make_float2(b0, b1), make_float2(c0, c1));
+    c0 = r.x;
+    c1 = r.y;
+}
+__device__ __forceinline__ void mul2(float a0, float a1, float b0, float b1, float& c0, float& c1) {
+    const float2 r = __fmul2_rn(make_float2(a0, a1), make_float2(b0, b1));
+    c0 = r.x;
+    c1 = r.y;
+}
+template <typename Real, int KP> struct Pairs {
+    static constexpr bool value = sizeof(Real) == 4 && KP % 2 == 0;
+};
+
 // D[u] = M L[u] with M given transposed (rows of T are columns of M).
 template <int KP, int SPT, typename Real>
 __device__ __forceinline__ void apply_t(const Real* T, const Real (&L)[SPT][KP], Real (&D)[SPT][KP]) {
@@ -512,25 +529,50 @@ __device__ __forceinline__ void apply_t(const Real* T, const Real (&L)[SPT][KP],
         Real row[KP];
         ld_vec<KP>(T + k * KP, row);
 #pragma unroll
-        for (int u = 0; u < SPT; ++u)
+        for (int u = 0; u < SPT; ++u) {
+            if constexpr (Pairs<Real, KP>::value) {
 #pragma unroll
-            for (int s = 0; s < KP; ++s) D[u][s] = fma(row[s], L[u][k], D[u][s]);
+                for (int s = 0; s < KP; s += 2)
+                    fma2(row[s], row[s + 1], L[u][k], L[u][k], D[u][s], D[u][s + 1]);
+            } else {
+#pragma unroll
+                for (int s = 0; s < KP; ++s) D[u][s] = fma(row[s], L[u][k], D[u][s]);
+            }
+        }
     }
 }
 
 // y[u] = M^T x[u] with M given transposed: y[k] = row_k(T) . x.
 template <int KP, int SPT, typename Real>
 __device__ __forceinline__ void apply_tt(const Real* T, const Real (&x)[SPT][KP], Real (&y)[SPT][KP]) {
+    if constexpr (Pairs<Real, KP>::value) {
+        // two rows at a time: y[u][k] and y[u][k+1] accumulate side by side
 #pragma unroll
-    for (int k = 0; k < KP; ++k) {
-        Real row[KP];
-        ld_vec<KP>(T + k * KP, row);
+        for (int k = 0; k < KP; k += 2) {
+            Real r0[KP], r1[KP];
+            ld_vec<KP>(T + k * KP, r0);
+            ld_vec<KP>(T + (k + 1) * KP, r1);
 #pragma unroll
-        for (int u = 0; u < SPT; ++u) {
-            Real acc = Real(0);
+            for (int u = 0; u < SPT; ++u) {
+                Real a0 = Real(0), a1 = Real(0);
 #pragma unroll
-            for (int s = 0; s < KP; ++s) acc = fma(row[s], x[u][s], acc);
-            y[u][k] = acc;
+                for (int s = 0; s < KP; ++s) fma2(r0[s], r1[s], x[u][s], x[u][s], a0, a1);
+                y[u][k] = a0;
+                y[u][k + 1] = a1;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < KP; ++k) {
+            Real row[KP];
+            ld_vec<KP>(T + k * KP, row);
+#pragma unroll
+            for (int u = 0; u < SPT; ++u) {
+                Real acc = Real(0);
+#pragma unroll
+                for (int s = 0; s < KP; ++s) acc = fma(row[s], x[u][s], acc);
+                y[u][k] = acc;
+            }
         }
     }
 }
@@ -728,9 +770,16 @@ prune_kernel(const PruneArgs a) {
             down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), Da);
             down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), Db);
 #pragma unroll
-            for (int u = 0; u < SPT; ++u)
+            for (int u = 0; u < SPT; ++u) {
+                if constexpr (Pairs<Real, KP>::value) {
 #pragma unroll
-                for (int k = 0; k < KP; ++k) Da[u][k] *= Db[u][k];
+                    for (int k = 0; k < KP; k += 2)
+                        mul2(Da[u][k], Da[u][k + 1], Db[u][k], Db[u][k + 1], Da[u][k], Da[u][k + 1]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < KP; ++k) Da[u][k] *= Db[u][k];
+                }
+            }
             rescale_warp<KP, Real, SPT>(Da, eacc);
             if (j + 1 < J) {
                 // the post-order column is only read back by the gradient sweep
@@ -816,9 +865,17 @@ prune_kernel(const PruneArgs a) {
                 // sibling's Down (turbo_mul!)
                 Real pt[SPT][KP];
 #pragma unroll
-                for (int u = 0; u < SPT; ++u)
+                for (int u = 0; u < SPT; ++u) {
+                    if constexpr (Pairs<Real, KP>::value) {
 #pragma unroll
-                    for (int k = 0; k < KP; ++k) pt[u][k] = pb[u][k] * D[1 - c][u][k];
+                        for (int k = 0; k < KP; k += 2)
+                            mul2(pb[u][k], pb[u][k + 1], D[1 - c][u][k], D[1 - c][u][k + 1],
+                                 pt[u][k], pt[u][k + 1]);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < KP; ++k) pt[u][k] = pb[u][k] * D[1 - c][u][k];
+                    }
+                }
                 if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
                     if (c == 0) down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
@@ -827,10 +884,16 @@ prune_kernel(const PruneArgs a) {
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
                         Real num = Real(0), den = Real(0);
+                        if constexpr (sizeof(Real) == 4) {
 #pragma unroll
-                        for (int k = 0; k < KP; ++k) {
-                            num = fma(pt[u][k], dD[u][k], num);
-                            den = fma(pt[u][k], D[c][u][k], den);
+                            for (int k = 0; k < KP; ++k)
+                                fma2(pt[u][k], pt[u][k], dD[u][k], D[c][u][k], num, den);
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < KP; ++k) {
+                                num = fma(pt[u][k], dD[u][k], num);
+                                den = fma(pt[u][k], D[c][u][k], den);
+                            }
                         }
                         g += valid[u] ? Real(wt[u]) * ratio(num, den) : Real(0);
                     }
