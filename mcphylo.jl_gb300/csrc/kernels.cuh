@@ -513,8 +513,10 @@ __device__ __forceinline__ void mul2(float a0, float a1, float b0, float b1, flo
     c0 = r.x;
     c1 = r.y;
 }
+// Used for the larger state spaces: at K <= 4 the pairing costs registers the
+// 4-sites-per-thread kernel does not have.
 template <typename Real, int KP> struct Pairs {
-    static constexpr bool value = sizeof(Real) == 4 && KP % 2 == 0;
+    static constexpr bool value = sizeof(Real) == 4 && KP % 2 == 0 && KP >= 8;
 };
 
 // D[u] = M L[u] with M given transposed (rows of T are columns of M).
@@ -884,7 +886,7 @@ prune_kernel(const PruneArgs a) {
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
                         Real num = Real(0), den = Real(0);
-                        if constexpr (sizeof(Real) == 4) {
+                        if constexpr (Pairs<Real, KP>::value) {
 #pragma unroll
                             for (int k = 0; k < KP; ++k)
                                 fma2(pt[u][k], pt[u][k], dD[u][k], D[c][u][k], num, den);
