@@ -199,18 +199,29 @@ __device__ __forceinline__ void leaf_down(uint32_t code, uint32_t allmask, const
     }
 }
 
-// (pt . x, pt . y) with four independent partial sums each
+// (pt . x, pt . y) with four independent partial sums each, the two dot products
+// side by side in packed FP32x2 FMAs (each lane rounds as the scalar FMA would)
 template <int KD>
 __device__ __forceinline__ void dot2(const float (&pt)[KD], const float (&x)[KD],
                                      const float (&y)[KD], float& nx, float& ny) {
-    float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
+    float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                     make_float2(0.f, 0.f)};
 #pragma unroll
-    for (int k = 0; k < KD; ++k) {
-        ax[k & 3] = fmaf(pt[k], x[k], ax[k & 3]);
-        ay[k & 3] = fmaf(pt[k], y[k], ay[k & 3]);
+    for (int k = 0; k < KD; ++k)
+        acc[k & 3] = __ffma2_rn(make_float2(pt[k], pt[k]), make_float2(x[k], y[k]), acc[k & 3]);
+    nx = (acc[0].x + acc[1].x) + (acc[2].x + acc[3].x);
+    ny = (acc[0].y + acc[1].y) + (acc[2].y + acc[3].y);
+}
+
+// v = a * b elementwise, in packed pairs
+template <int KD>
+__device__ __forceinline__ void mul_v(const float (&a)[KD], const float (&b)[KD], float (&v)[KD]) {
+#pragma unroll
+    for (int k = 0; k < KD; k += 2) {
+        const float2 r = __fmul2_rn(make_float2(a[k], a[k + 1]), make_float2(b[k], b[k + 1]));
+        v[k] = r.x;
+        v[k + 1] = r.y;
     }
-    nx = (ax[0] + ax[1]) + (ax[2] + ax[3]);
-    ny = (ay[0] + ay[1]) + (ay[2] + ay[3]);
 }
 
 // This thread's row of an A tile: VK values, zero beyond (TF32-rounded or BF16).
@@ -439,8 +450,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             if (op1 < 0)
                 leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
                               reinterpret_cast<const float*>(f1 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D1);
-#pragma unroll
-            for (int k = 0; k < KD; ++k) D0[k] *= D1[k];
+            mul_v<VK>(D0, D1, D0);
             eacc += rescale<VK, float>(D0);
             if (j + 1 < J) {
                 // TF32 copy in operand layout for the steps that read it back; the
@@ -449,11 +459,11 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 write_a<VK, FMT>(post + size_t(j) * TILE, t, D0);
                 if (hd[14] >= 0) fence_proxy_async_global();
 #pragma unroll
-                for (int k = 0; k < KD; ++k) Lp[k] = D0[k];
+                for (int k = 0; k < VK; ++k) Lp[k] = D0[k];
             } else {
                 float lik = 0.f;
 #pragma unroll
-                for (int k = 0; k < KD; ++k)
+                for (int k = 0; k < VK; ++k)
                     if (k < K) lik = fmaf(float(__ldg(pi_d + k)), D0[k], lik);
                 const int ex = int(eacc) - J * 127;
                 ll += valid ? wt * (log(double(lik)) + double(ex) * LN2) : 0.0;
@@ -525,7 +535,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         }
         float pb[VK];
 #pragma unroll
-        for (int k = 0; k < KD; ++k) pb[k] = (k < K) ? float(__ldg(pi_d + k)) : 0.f;
+        for (int k = 0; k < VK; ++k) pb[k] = (k < K) ? float(__ldg(pi_d + k)) : 0.f;
         for (int j = J - 1; j >= 0; --j) {
             const int b = (J - 1 - j) & 1;
             const unsigned char* R = rec(b);
@@ -570,8 +580,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                                   reinterpret_cast<const float*>(k1 + 2 * tc_tile(K, FMT) + tc_tab(K)), K,
                                   K4, dD);
                 }
-#pragma unroll
-                for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D0[k];
+                mul_v<VK>(pb, D0, pt);
                 float num, den;
                 dot2<VK>(pt, dD, D1, num, den);
                 g1 = valid ? wtf * __fdividef(num, den) : 0.f;
@@ -586,8 +595,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                                   reinterpret_cast<const float*>(k0 + 2 * tc_tile(K, FMT) + tc_tab(K)), K,
                                   K4, dD);
                 }
-#pragma unroll
-                for (int k = 0; k < KD; ++k) pt[k] = pb[k] * D1[k];
+                mul_v<VK>(pb, D1, pt);
                 float num, den;
                 dot2<VK>(pt, dD, D0, num, den);
                 g0 = valid ? wtf * __fdividef(num, den) : 0.f;
@@ -632,7 +640,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 }
             }
 #pragma unroll
-            for (int k = 0; k < KD; ++k) pb[k] = pbn[k];
+            for (int k = 0; k < VK; ++k) pb[k] = pbn[k];
             code0 = ncode0;
             code1 = ncode1;
             // end of step
