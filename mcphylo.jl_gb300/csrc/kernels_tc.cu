@@ -199,29 +199,25 @@ __device__ __forceinline__ void leaf_down(uint32_t code, uint32_t allmask, const
     }
 }
 
-// (pt . x, pt . y) with four independent partial sums each, the two dot products
-// side by side in packed FP32x2 FMAs (each lane rounds as the scalar FMA would)
+// (pt . x, pt . y) with four independent partial sums each
 template <int KD>
 __device__ __forceinline__ void dot2(const float (&pt)[KD], const float (&x)[KD],
                                      const float (&y)[KD], float& nx, float& ny) {
-    float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
-                     make_float2(0.f, 0.f)};
+    float ax[4] = {0.f, 0.f, 0.f, 0.f}, ay[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int k = 0; k < KD; ++k)
-        acc[k & 3] = __ffma2_rn(make_float2(pt[k], pt[k]), make_float2(x[k], y[k]), acc[k & 3]);
-    nx = (acc[0].x + acc[1].x) + (acc[2].x + acc[3].x);
-    ny = (acc[0].y + acc[1].y) + (acc[2].y + acc[3].y);
+    for (int k = 0; k < KD; ++k) {
+        ax[k & 3] = fmaf(pt[k], x[k], ax[k & 3]);
+        ay[k & 3] = fmaf(pt[k], y[k], ay[k & 3]);
+    }
+    nx = (ax[0] + ax[1]) + (ax[2] + ax[3]);
+    ny = (ay[0] + ay[1]) + (ay[2] + ay[3]);
 }
 
-// v = a * b elementwise, in packed pairs
+// v = a * b elementwise
 template <int KD>
 __device__ __forceinline__ void mul_v(const float (&a)[KD], const float (&b)[KD], float (&v)[KD]) {
 #pragma unroll
-    for (int k = 0; k < KD; k += 2) {
-        const float2 r = __fmul2_rn(make_float2(a[k], a[k + 1]), make_float2(b[k], b[k + 1]));
-        v[k] = r.x;
-        v[k + 1] = r.y;
-    }
+    for (int k = 0; k < KD; ++k) v[k] = a[k] * b[k];
 }
 
 // This thread's row of an A tile: VK values, zero beyond (TF32-rounded or BF16).
