@@ -13,9 +13,10 @@ Default workload: 256 independent HKY+G4 instances of uneven size in one launch
 (T ~ logU[16, 1024] taxa, S ~ logU[500, 50000] sites, kappa ~ LogNormal(1, 0.5)),
 FP32-scaled path, compared with the plain FP64 GPU path on the same inputs.
 
-value: device-resident inputs (branch lengths already in HBM), CUDA events on the
-engine's stream around each step, L2 flushed (512 MB write) between steps outside
-the events.  e2e: the same step through the C ABI with host buffers (branch
+value: device-resident inputs (branch lengths already in HBM), each evaluation
+replayed as one captured CUDA graph, CUDA events on the engine's stream around
+each step, L2 flushed (512 MB write) between steps outside the events; per-kernel
+times come from a separate pass with the engine's own events.  e2e: the same step through the C ABI with host buffers (branch
 lengths in, ll and gradient out, copies inside the timed region).
 --impl reference: the CPU restatement of the reference's loops (FP64, OpenMP, all
 host cores) on a bounded sample of the same workload each step.
@@ -451,40 +452,65 @@ def run_gpu(args, rank, world):
     d_grad = torch.zeros(G, dtype=torch.float64, device="cuda")
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 512 MB > L2
 
-    def dev_step(k):
-        e.set_all_branch_lengths_device(dev_sets[k].data_ptr())
+    def dev_step(eng, k):
+        eng.set_all_branch_lengths_device(dev_sets[k % nsets].data_ptr())
         if args.mode == "grad":
-            e.logpdf_grad_device(d_ll.data_ptr(), d_grad.data_ptr())
+            eng.logpdf_grad_device(d_ll.data_ptr(), d_grad.data_ptr())
         else:
-            e.logpdf_device(d_ll.data_ptr())
+            eng.logpdf_device(d_ll.data_ptr())
+
+    def time_steps(eng, n, first):
+        """Device time of n evaluations (graph replays, no per-kernel events), each
+        bracketed by CUDA events on the engine's stream, L2 flushed before each."""
+        eng.set_stream(stream.cuda_stream)
+        eng.enable_timing(False)
+        eng.enable_graph(True)
+        for k in range(args.warmup):
+            flush.zero_()
+            dev_step(eng, first + k)
+        eng.synchronize()
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        for i in range(n):
+            flush.zero_()
+            st[i].record(stream)
+            dev_step(eng, first + args.warmup + i)
+            en[i].record(stream)
+        eng.synchronize()
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in zip(st, en)]
+
+    def phase_times(eng, n, first):
+        """Per-kernel device times (the engine's own events, eager launches)."""
+        eng.set_stream(stream.cuda_stream)
+        eng.enable_graph(False)
+        eng.enable_timing(True)
+        rows = []
+        for i in range(n):
+            flush.zero_()
+            dev_step(eng, first + i)
+            eng.synchronize()
+            rows.append(eng.timing())
+        eng.enable_timing(False)
+        return rows
 
     for k in range(args.warmup):
         flush.zero_()
-        dev_step(k)
+        dev_step(e, k)
     e.synchronize()
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    prune_ms, build_ms, red_ms = [], [], []
-    ll32 = []
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
-            dev_step(args.warmup + i)
-            ends[i].record(stream)
-            e.synchronize()
-            t = e.timing()
-            prune_ms.append(t["prune_ms"])
-            build_ms.append(t["build_p_ms"])
-            red_ms.append(t["reduce_ms"])
-        torch.cuda.synchronize()
+        step_ms = time_steps(e, args.steps, 0)
         wall = time.perf_counter() - wall0
     clocks = clk.summary()
-    step_ms = [s.elapsed_time(t) for s, t in zip(starts, ends)]
+    launches = e.counts()["launches"]
+    ph = phase_times(e, max(3, min(args.steps, 10)), 0)
+    prune_ms = [t["prune_ms"] for t in ph]
+    build_ms = [t["build_p_ms"] for t in ph]
+    red_ms = [t["reduce_ms"] for t in ph]
     assert min(step_ms) >= 0.9 * statistics.mean(prune_ms), "events did not bracket the step"
     ms = statistics.mean(step_ms)
     if dist is not None:
@@ -492,6 +518,9 @@ def run_gpu(args, rank, world):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     value = units * world / (ms / 1e3)
+    # results of the timed region's last step (the phase pass reran earlier sets)
+    dev_step(e, args.warmup + args.steps - 1)
+    e.synchronize()
     ll32_last = d_ll.cpu().numpy().copy()
     g32_last = d_grad.cpu().numpy().copy()
 
@@ -532,24 +561,13 @@ def run_gpu(args, rank, world):
     err = None
     if not args.no_fp64:
         e64 = make_engine(insts, "f64")
-        e64.enable_timing(True)
         last = host_sets[args.warmup + args.steps - 1]
         e64.set_all_branch_lengths(last)
         if args.mode == "grad":
             ll64, g64 = e64.logpdf_grad()
         else:
             ll64, g64 = e64.logpdf(), None
-        t64 = []
-        for _ in range(args.fp64_steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            if args.mode == "grad":
-                e64.logpdf_grad()
-            else:
-                e64.logpdf()
-            tm = e64.timing()
-            t64.append(tm["build_p_ms"] + tm["prune_ms"] + tm["reduce_ms"])
-        ms64 = statistics.mean(t64)
+        ms64 = statistics.mean(time_steps(e64, args.fp64_steps, 0))
         fp64 = {"value": units * world / (ms64 / 1e3), "ms_per_step": ms64,
                 "speedup_fp32_over_fp64": (units / (ms / 1e3)) / (units / (ms64 / 1e3))}
         ll64 = np.atleast_1d(ll64)
@@ -572,17 +590,7 @@ def run_gpu(args, rank, world):
     if tc_path:
         e32 = make_engine(insts, "f32")
         e32.autotune()
-        e32.enable_timing(True)
-        e32.set_all_branch_lengths(host_sets[args.warmup + args.steps - 1])
-        e32.logpdf_grad() if args.mode == "grad" else e32.logpdf()
-        t32 = []
-        for _ in range(args.fp64_steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            e32.logpdf_grad() if args.mode == "grad" else e32.logpdf()
-            tm = e32.timing()
-            t32.append(tm["build_p_ms"] + tm["prune_ms"] + tm["reduce_ms"])
-        ms32 = statistics.mean(t32)
+        ms32 = statistics.mean(time_steps(e32, args.fp64_steps, 0))
         simt = {"value": units * world / (ms32 / 1e3), "ms_per_step": ms32,
                 "speedup_tensor_over_simt": ms32 / ms}
         e32.close()
@@ -646,7 +654,7 @@ def run_gpu(args, rank, world):
                           l2="flushed between steps (512 MB write, outside the timed events)",
                           parallelism="replicas" if world > 1 else "single GPU"),
            "clocks": clocks, "e2e": e2e,
-           "gpu_launches": (4 if args.mode == "grad" else 4) * args.steps,
+           "gpu_launches": launches * args.steps,
            "roofline": roofline, "cpu_baseline": cpu, "fp64_plain": fp64,
            "error_vs_fp64": err, "fp32_simt": simt,
            "kernel_ms": {"build_transition": statistics.mean(build_ms), "prune": pr,

@@ -177,16 +177,18 @@ int mcphy_tc_selftest(int64_t kd, int64_t n, int bf16, const float* a, const flo
 int mcphy_set_stream(mcphy_handle h, void* stream);
 int mcphy_synchronize(mcphy_handle h);
 /* Launch shape of the fused pruning kernel: sites per thread (1, 2 or 4) and
- * threads per block (64..1024, multiple of 32); 0 keeps the automatic choice. */
+ * threads per block (64..256, multiple of 32); 0 keeps the automatic choice. */
 int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block);
 /* Picks the fused kernel's launch shape for the current problem: times each
  * candidate (sites per thread x threads per block) on full evaluations and keeps
  * the fastest; out2 (may be NULL) receives it.  No counterpart in the reference
  * (its @tturbo loops are tuned by LoopVectorization at compile time). */
 int mcphy_autotune(mcphy_handle h, int* out2);
-/* Replays every host-API evaluation as one captured CUDA graph (fused sweep,
- * reduction and result copies), re-captured when the layout changes.  Per-kernel
- * timing is not collected while on.  No counterpart in the reference. */
+/* Replays every evaluation as one captured CUDA graph: the record build, fused
+ * sweep and reduction, plus the result copies for the host entry points.  One
+ * graph per entry-point kind and mode, re-captured when the layout changes (a
+ * topology change on the same leaves keeps it).  Per-kernel timing is not
+ * collected while on.  No counterpart in the reference. */
 int mcphy_enable_graph(mcphy_handle h, int on);
 /* Per-call device timing (CUDA events around each kernel of the last evaluation),
  * milliseconds: [0] P/dP build, [1] fused pruning kernel, [2] reduction. */

@@ -543,12 +543,12 @@ int run(mcphy_engine* h, bool want_grad) {
     b.K = h->K;
     b.Kp = h->Kp;
     b.C = h->C;
+    b.counter = static_cast<int32_t*>(h->d_counter.p);   // zeroed for the sweep
     const int fmt = tc_fmt(h);
     const bool tc = fmt >= 0;
     CK(tc ? launch_build_records_tc(fmt, b, st) : launch_build_records(f64, b, st));
     if (h->timing) CK(cudaEventRecord(h->ev[1], st));
 
-    CK(cudaMemsetAsync(h->d_counter.p, 0, 2 * sizeof(int32_t), st));
     PruneArgs a{};
     a.inst = b.inst;
     a.items = static_cast<const int2*>(h->d_items.p);
@@ -592,7 +592,7 @@ int run(mcphy_engine* h, bool want_grad) {
     r.out = static_cast<double*>(h->d_out.p);
     CK(launch_reduce(f64, r, h->max_branch, st));
     if (h->timing) CK(cudaEventRecord(h->ev[3], st));
-    h->counts[0] = 4;   // build_records, prune, reduce_pass1, reduce_pass2
+    h->counts[0] = 2 + reduce_launches(h->n_split);   // build_records, prune, reduction
     h->counts[1] = h->units;
     return MCPHY_OK;
 }
@@ -616,22 +616,25 @@ int enqueue_eval(mcphy_engine* h, bool want_grad) {
     return MCPHY_OK;
 }
 
-// Captures enqueue_eval into a CUDA graph (once per layout and mode).
-int graph_for(mcphy_engine* h, bool want_grad, cudaGraphExec_t* out) {
-    cudaGraphExec_t& ex = h->graph_exec[want_grad ? 1 : 0];
+// Captures one evaluation into a CUDA graph (once per layout and mode): with the
+// copies of its results into the pinned output buffer (host entry points), or the
+// kernels alone, results left in d_out (device entry points).
+int graph_for(mcphy_engine* h, bool want_grad, bool device, cudaGraphExec_t* out) {
+    cudaGraphExec_t& ex = h->graph_exec[(device ? 2 : 0) + (want_grad ? 1 : 0)];
+    auto enqueue = [&]() { return device ? run(h, want_grad) : enqueue_eval(h, want_grad); };
     if (!ex) {
         const bool timing = h->timing;
         h->timing = false;
         // one eager evaluation first, so that every launch-time setting (kernel
         // attributes) is made outside the capture
-        int rc0 = enqueue_eval(h, want_grad);
+        int rc0 = enqueue();
         if (rc0) {
             h->timing = timing;
             return rc0;
         }
         CK(cudaStreamSynchronize(h->stream));
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_eval(h, want_grad);
+        int rc = enqueue();
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(h->stream, &g);
         h->timing = timing;
@@ -662,9 +665,9 @@ int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
     *flag = 0;
     if (h->use_graph && !h->timing && h->inject != 1) {
         cudaGraphExec_t ex = nullptr;
-        if ((rc = graph_for(h, want_grad, &ex))) return rc;
+        if ((rc = graph_for(h, want_grad, false, &ex))) return rc;
         CK(cudaGraphLaunch(ex, h->stream));
-        h->counts[0] = 4;
+        h->counts[0] = 2 + reduce_launches(h->n_split);
         h->counts[1] = h->units;
     } else {
         if ((rc = enqueue_eval(h, want_grad))) return rc;
@@ -676,6 +679,21 @@ int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
     std::memcpy(ll, h->h_out, sizeof(double) * h->M);
     if (want_grad) std::memcpy(grad, h->h_out + h->M, sizeof(double) * h->total_branch);
     return MCPHY_OK;
+}
+
+// Device entry points: the kernels of one evaluation, replayed from a captured
+// graph when graphs are on (results in d_out).
+int run_device(mcphy_engine* h, bool want_grad) {
+    if (h->use_graph && !h->timing && h->inject != 1) {
+        cudaGraphExec_t ex = nullptr;
+        int rc;
+        if ((rc = graph_for(h, want_grad, true, &ex))) return rc;
+        CK(cudaGraphLaunch(ex, h->stream));
+        h->counts[0] = 2 + reduce_launches(h->n_split);
+        h->counts[1] = h->units;
+        return MCPHY_OK;
+    }
+    return run(h, want_grad);
 }
 
 int set_data_common(mcphy_engine* h, int64_t i, int64_t nsites, int64_t nnodes,
@@ -1029,7 +1047,7 @@ int mcphy_logpdf_grad_device(mcphy_handle h, double* d_ll, double* d_grad_packed
     if (!d_ll || !d_grad_packed) return fail(h, MCPHY_ERR_ARG, "NULL output");
     int rc;
     if ((rc = prepare(h))) return rc;
-    if ((rc = run(h, true))) return rc;
+    if ((rc = run_device(h, true))) return rc;
     CK(cudaMemcpyAsync(d_ll, h->d_out.p, sizeof(double) * size_t(h->M), cudaMemcpyDeviceToDevice,
                        h->stream));
     CK(cudaMemcpyAsync(d_grad_packed, static_cast<double*>(h->d_out.p) + h->M,
@@ -1043,7 +1061,7 @@ int mcphy_logpdf_device(mcphy_handle h, double* d_ll) {
     if (!d_ll) return fail(h, MCPHY_ERR_ARG, "NULL output");
     int rc;
     if ((rc = prepare(h))) return rc;
-    if ((rc = run(h, false))) return rc;
+    if ((rc = run_device(h, false))) return rc;
     CK(cudaMemcpyAsync(d_ll, h->d_out.p, sizeof(double) * size_t(h->M), cudaMemcpyDeviceToDevice,
                        h->stream));
     return MCPHY_OK;

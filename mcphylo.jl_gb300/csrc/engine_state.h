@@ -92,7 +92,8 @@ struct mcphy_engine {
     int inject = 0;
     // CUDA graph replay of a whole evaluation (fused sweep + reduction + copies)
     bool use_graph = false;
-    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};   // [logL only, logL + gradient]
+    // [logL only, logL + gradient] x [host entry points, device entry points]
+    cudaGraphExec_t graph_exec[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t h_out_cap = 0;
 
     bool timing = false;

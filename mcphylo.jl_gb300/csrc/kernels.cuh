@@ -168,6 +168,8 @@ struct BuildRecArgs {
     int32_t K;
     int32_t Kp;
     int32_t C;
+    int32_t* counter;         // when set, thread 0 zeroes the sweep's work counter and
+                              // error flag (the sweep runs after this kernel)
 };
 
 struct ReduceArgs {
@@ -947,6 +949,10 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, Kp = a.Kp, C = a.C;
     const int R = rec_row_threads(Kp);
+    if (tid == 0 && a.counter) {
+        a.counter[0] = 0;
+        a.counter[1] = 0;
+    }
     if (tid >= int64_t(a.n_steps) * 2 * C * R) return;
     const int s0 = int(tid % R);
     const int64_t u = tid / R;
@@ -1040,6 +1046,7 @@ cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, int* blocks_per_sm);
 cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, int* blocks_per_sm);
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st);
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st);
+int reduce_launches(int n_split);   // kernels launch_reduce launches
 
 // ---------------------------------------------------------------- leaf-code gather
 // Rebuilds one instance's schedule-ordered leaf codes from its leaf-major copy

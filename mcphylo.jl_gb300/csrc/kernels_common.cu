@@ -64,23 +64,28 @@ __global__ void reduce_pass2(const ReduceArgs a) {
     a.out[e] = s;
 }
 
+int reduce_launches(int n_split) { return n_split > 1 ? 2 : 1; }
+
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st) {
     dim3 grid(unsigned((max_branch + 31) / 32 + 1), unsigned(a.n_inst), unsigned(a.n_split));
     dim3 block(32, RY);
+    // one split: the first pass's sums are the results (its row layout is the output's)
+    ReduceArgs a1 = a;
+    if (a.n_split == 1) a1.part = a.out;
     if (f64)
-        reduce_pass1<double><<<grid, block, 0, st>>>(a);
+        reduce_pass1<double><<<grid, block, 0, st>>>(a1);
     else
-        reduce_pass1<float><<<grid, block, 0, st>>>(a);
+        reduce_pass1<float><<<grid, block, 0, st>>>(a1);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || a.n_split == 1) return e;
     const int64_t n = int64_t(a.n_inst) + a.total_branch;
     reduce_pass2<<<unsigned((n + 255) / 256), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st) {
-    const int64_t total = int64_t(a.n_steps) * 2 * a.C * rec_row_threads(a.Kp);
-    if (total == 0) return cudaSuccess;
+    // at least one thread: it also zeroes the sweep's counter
+    const int64_t total = std::max<int64_t>(1, int64_t(a.n_steps) * 2 * a.C * rec_row_threads(a.Kp));
     const int tpb = 128;
     const int64_t blocks = (total + tpb - 1) / tpb;
     if (f64)

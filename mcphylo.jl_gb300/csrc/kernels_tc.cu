@@ -58,6 +58,10 @@ template <int FMT>
 __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, C = a.C;
+    if (tid == 0 && a.counter) {
+        a.counter[0] = 0;
+        a.counter[1] = 0;
+    }
     if (tid >= int64_t(a.n_steps) * 2 * C * TC_N) return;
     const int s = int(tid % TC_N);
     const int64_t u = tid / TC_N;
@@ -721,8 +725,7 @@ cudaError_t occ_tc(int K, int* bps) {
 }  // namespace
 
 cudaError_t launch_build_records_tc(int fmt, const BuildRecArgs& a, cudaStream_t st) {
-    const int64_t total = int64_t(a.n_steps) * 2 * a.C * TC_N;
-    if (total == 0) return cudaSuccess;
+    const int64_t total = std::max<int64_t>(1, int64_t(a.n_steps) * 2 * a.C * TC_N);
     const int tpb = 128;
     const unsigned blocks = unsigned((total + tpb - 1) / tpb);
     if (fmt) build_records_tc_kernel<1><<<blocks, tpb, 0, st>>>(a);

@@ -371,6 +371,51 @@ def test_graph_replay_matches_eager(built_lib):
     assert got[0] == want[0] and np.array_equal(got[1], want[1])
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_device_entry_graph_replay_matches_eager(built_lib, precision):
+    """The device entry points replay one captured graph per mode when graphs are
+    on: results equal eager launches bit for bit over new branch lengths, a
+    topology change on the same leaves and logL-only calls in between; the oracle
+    checks the eager results."""
+    torch = pytest.importorskip("torch")
+    inst = random_instance(4, 4, 40, 700, seed=44)
+    rng = np.random.default_rng(2)
+    parent_b = _nni(inst.parent, rng)
+    sets = [inst.blen * rng.uniform(0.8, 1.2, size=inst.blen.shape) for _ in range(3)]
+    d_sets = [torch.tensor(b, dtype=torch.float64, device="cuda") for b in sets]
+    G = len(inst.blen)
+    runs = []
+    for graph in (False, True):
+        e = engine(inst, precision)
+        e.enable_graph(graph)
+        d_ll = torch.zeros(1, dtype=torch.float64, device="cuda")
+        d_l2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        d_g = torch.zeros(G, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        out = []
+        for k, d_b in enumerate(d_sets):
+            if k == 1:
+                e.set_tree(parent_b, inst.blen)
+            e.set_all_branch_lengths_device(d_b.data_ptr())
+            e.logpdf_grad_device(d_ll.data_ptr(), d_g.data_ptr())
+            e.synchronize()
+            ll, g = d_ll.cpu().numpy().copy(), d_g.cpu().numpy().copy()
+            e.logpdf_device(d_l2.data_ptr())
+            e.synchronize()
+            out.append((ll, g, d_l2.cpu().numpy().copy()))
+        assert e.counts()["launches"] in (3, 4)
+        e.close()
+        runs.append(out)
+    for (ll0, g0, l0), (ll1, g1, l1) in zip(*runs):
+        assert np.array_equal(ll0, ll1) and np.array_equal(g0, g1) and np.array_equal(l0, l1)
+        assert np.array_equal(ll0, l0)
+    b = simulate.Instance(T.from_parent(parent_b, sets[2]), parent_b, sets[2], inst.leaf_nums,
+                          inst.codes, inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
+    llo, go = oracle(b)
+    rtol = F64_RTOL if precision == "f64" else F32_LL_RTOL
+    assert abs(runs[0][2][0][0] - llo) <= rtol * abs(llo)
+
+
 def test_autotune_keeps_results(built_lib):
     inst = random_instance(4, 4, 50, 2000, seed=45)
     e = engine(inst, "f32")
