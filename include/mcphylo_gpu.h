@@ -179,9 +179,29 @@ int mcphy_synchronize(mcphy_handle h);
 /* Launch shape of the fused pruning kernel: sites per thread (1, 2 or 4) and
  * threads per block (64..256, multiple of 32); 0 keeps the automatic choice. */
 int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block);
+/* Sweep of the SIMT paths (no counterpart in the reference).
+ *   MCPHY_SWEEP_WALK:  every warp walks the whole tree for its 32 x sites_per_thread
+ *                      sites (throughput: many site blocks);
+ *   MCPHY_SWEEP_LEVEL: a CTA's warps share the tree of one 32-site block level by
+ *                      level, everything in shared memory (latency: few site blocks,
+ *                      small trees; K <= 8, schedules that fit one CTA);
+ *   MCPHY_SWEEP_AUTO:  the level sweep when it fits, no sites_per_thread was set and
+ *                      the problem has at most two 32-site work items per SM, else
+ *                      the tree walk (default).
+ * Same results up to rounding.  MCPHY_ERR_ARG for an unknown kind; a level sweep
+ * that does not fit falls back to the tree walk.  mcphy_get_sweep reports the
+ * sweep of the current layout (laying it out first if needed). */
+enum {
+    MCPHY_SWEEP_AUTO = 0,
+    MCPHY_SWEEP_WALK = 1,
+    MCPHY_SWEEP_LEVEL = 2
+};
+int mcphy_set_sweep(mcphy_handle h, int sweep);
+int mcphy_get_sweep(mcphy_handle h, int* sweep);
 /* Picks the fused kernel's launch shape for the current problem: times each
- * candidate (sites per thread x threads per block) on full evaluations and keeps
- * the fastest; out2 (may be NULL) receives it.  No counterpart in the reference
+ * candidate (sweep, sites per thread, threads per block) on full evaluations and
+ * keeps the fastest (sweep and reduction time); out2 (may be NULL) receives sites
+ * per thread and threads per block, mcphy_get_sweep the sweep.  No counterpart in the reference
  * (its @tturbo loops are tuned by LoopVectorization at compile time). */
 int mcphy_autotune(mcphy_handle h, int* out2);
 /* Replays every evaluation as one captured CUDA graph: the record build, fused
@@ -201,7 +221,8 @@ const char* mcphy_last_error(mcphy_handle h);
 /* Test hook, no counterpart in the reference.  kind 1 makes the next evaluation's
  * first staging wait run out (its copy is never issued) so that the bounded-wait
  * path can be tested without a device fault; that evaluation returns
- * MCPHY_ERR_TIMEOUT and later ones are unaffected.  kind 2 makes the next device
+ * MCPHY_ERR_TIMEOUT and later ones are unaffected (tree-walk and tensor-core sweeps;
+ * the level sweep stages nothing and has no waits).  kind 2 makes the next device
  * allocation fail (MCPHY_ERR_OOM); the handle keeps its state and the next call
  * retries.  kind 0 clears either. */
 int mcphy_debug_inject(mcphy_handle h, int kind);

@@ -114,13 +114,35 @@ int tc_fmt(const mcphy_engine* h) {
     return h->prec == MCPHY_PREC_TF32 ? 0 : h->prec == MCPHY_PREC_BF16 ? 1 : -1;
 }
 
-// Chooses the fused kernel's launch shape.
+// Level-synchronous sweep: supported state spaces, and whether a CTA's shared
+// memory holds an item of the largest schedule.
+bool level_fits(const mcphy_engine* h, int tpb) {
+    return tc_fmt(h) < 0 && level_supported(h->Kp) &&
+           level_smem_bytes(h->Kp, int(real_size(h)), h->max_J_hint, tpb / 32) <= kLevelSmemMax;
+}
+
+// Chooses the sweep and the launch shape.
 void choose_tiles(mcphy_engine* h) {
+    h->sweep = MCPHY_SWEEP_WALK;
     if (tc_fmt(h) >= 0) {
         // one CTA of 128 threads per 128-site work item (4 x 32 sites)
         h->spt = 4;
         h->tpb = TC_M;
         return;
+    }
+    // small problems (a few 32-site blocks, small trees) are latency-bound in the
+    // tree walk: share each tree among a CTA's warps, level by level
+    const int ltpb = h->tpb_req ? h->tpb_req : 128;
+    const bool level_ok = level_fits(h, ltpb);
+    if (h->sweep_req == MCPHY_SWEEP_LEVEL ||
+        (h->sweep_req == 0 && h->spt_req == 0 && level_ok &&
+         h->items_hint <= int64_t(2) * h->sm_count)) {
+        if (level_ok) {
+            h->sweep = MCPHY_SWEEP_LEVEL;
+            h->spt = 1;
+            h->tpb = ltpb;
+            return;
+        }
     }
     int spt = h->spt_req;
     if (spt == 0) spt = 1;
@@ -149,6 +171,14 @@ void drop_graphs(mcphy_engine* h) {
 int layout(mcphy_engine* h) {
     Range nv("mcphy_layout");
     drop_graphs(h);
+    // sizes the sweep choice needs before the schedules exist: the binarised tree
+    // of n leaves has n - 1 steps; work items of 32-site blocks
+    h->max_J_hint = 0;
+    h->items_hint = 0;
+    for (const Inst& in : h->inst) {
+        h->max_J_hint = std::max<int32_t>(h->max_J_hint, int32_t(in.leaf_nums.size()) - 1);
+        h->items_hint += int64_t(h->C) * ((in.S + 31) / 32);
+    }
     choose_tiles(h);
     const int SB = 32 * h->spt;
     const int K = h->K, Kp = h->Kp, C = h->C;
@@ -167,8 +197,9 @@ int layout(mcphy_engine* h) {
     int64_t sched_off = 0, rec_off = 0, leaf_off = 0, param_off = 0, item_off = 0,
             pgrad_off = 0, blen_off = 0, nsteps = 0;
     const int64_t psize = param_size(K, Kp, C);
-    int64_t lc_off = 0, w_off = 0;
+    int64_t lc_off = 0, w_off = 0, plan_off = 0;
     h->lc_off.assign(h->M, 0);
+    h->plan_all.clear();
     for (int64_t i = 0; i < h->M; ++i) {
         Inst& in = h->inst[i];
         in.topo_dirty = false;
@@ -210,6 +241,10 @@ int layout(mcphy_engine* h) {
         d.grad_off = blen_off;
         h->sched_all.insert(h->sched_all.end(), sc.nodes.begin(), sc.nodes.end());
         sched_off += sc.J;
+        d.plan_off = plan_off;
+        h->plan_all.resize(size_t(plan_off + 2 * sc.J + 2), 0);
+        build_level_plan(sc.nodes.data(), sc.J, h->plan_all.data() + plan_off);
+        plan_off += 2 * int64_t(sc.J) + 2;
         rec_off += int64_t(C) * sc.J * rbytes;
         // code leaves: the leaf codes arranged in schedule order, [block][step][operand][32*spt]
         // (internal operands leave their entries unused); dense leaves: [row][S_pad][Kp]
@@ -268,6 +303,7 @@ int layout(mcphy_engine* h) {
     int rc;
     if ((rc = ensure(h, h->d_desc, sizeof(InstanceDesc) * h->M))) return rc;
     if ((rc = ensure(h, h->d_sched, sizeof(SchedNode) * h->sched_all.size()))) return rc;
+    if ((rc = ensure(h, h->d_plan, sizeof(int32_t) * h->plan_all.size()))) return rc;
     if ((rc = ensure(h, h->d_items, sizeof(int2) * items.size()))) return rc;
     if ((rc = ensure(h, h->d_queue, sizeof(int32_t) * queue.size()))) return rc;
     if ((rc = ensure(h, h->d_steps, sizeof(int2) * steps.size()))) return rc;
@@ -296,22 +332,31 @@ int layout(mcphy_engine* h) {
     CK(cudaMemcpy(h->d_desc.p, h->desc.data(), sizeof(InstanceDesc) * h->M, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_sched.p, h->sched_all.data(), sizeof(SchedNode) * h->sched_all.size(),
                   cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_plan.p, h->plan_all.data(), sizeof(int32_t) * h->plan_all.size(),
+                  cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_items.p, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_queue.p, queue.data(), sizeof(int32_t) * queue.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(h->d_steps.p, steps.data(), sizeof(int2) * steps.size(), cudaMemcpyHostToDevice));
 
     // persistent grid: as many resident warps as the SMs hold, never more than items
+    const bool level = h->sweep == MCPHY_SWEEP_LEVEL;
     int bps = 0;
     cudaError_t oe = tc ? occupancy_prune_tc(fmt, K, &bps)
-                        : (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
-                                                      : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
+                     : level ? occupancy_prune_level(h->prec == MCPHY_PREC_F64, Kp, h->tpb, h->max_J, &bps)
+                     : (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
+                                                   : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
     if (oe != cudaSuccess || bps < 1) bps = 1;
-    // scratch columns: per warp (SIMT kernels) or per 128-thread CTA (tensor cores)
-    const int wpb = tc ? 1 : h->tpb / 32;
+    // work items per CTA at a time: one per warp (tree walk), one per CTA otherwise;
+    // scratch columns: per warp (tree walk) or per 128-thread CTA (tensor cores)
+    const int wpb = (tc || level) ? 1 : h->tpb / 32;
     int64_t blocks = int64_t(bps) * h->sm_count;
     blocks = std::min<int64_t>(blocks, (h->n_items + wpb - 1) / wpb);
     blocks = std::max<int64_t>(blocks, 1);
-    if (tc) {
+    if (level) {
+        // everything of an item lives in shared memory
+        h->warp_stride = 0;
+        h->pre_warp_stride = 0;
+    } else if (tc) {
         // post: [step][A tile] in 4-byte units; pre: [slot][K][128] floats
         h->warp_stride = int64_t(h->max_J) * tc_atile(K, fmt) / 4;
         h->pre_warp_stride = int64_t(h->max_pre) * K * TC_M;
@@ -460,6 +505,10 @@ int retopo(mcphy_engine* h) {
         CK(cudaMemcpyAsync(static_cast<SchedNode*>(h->d_sched.p) + d.sched_off,
                            h->sched_all.data() + d.sched_off, sizeof(SchedNode) * size_t(d.J),
                            cudaMemcpyHostToDevice, h->stream));
+        const int np = build_level_plan(t.second.nodes.data(), d.J, h->plan_all.data() + d.plan_off);
+        CK(cudaMemcpyAsync(static_cast<int32_t*>(h->d_plan.p) + d.plan_off,
+                           h->plan_all.data() + d.plan_off, sizeof(int32_t) * size_t(np),
+                           cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(static_cast<InstanceDesc*>(h->d_desc.p) + i, &h->desc[i],
                            sizeof(InstanceDesc), cudaMemcpyHostToDevice, h->stream));
         if ((rc = gather_instance(h, i))) return rc;
@@ -573,8 +622,11 @@ int run(mcphy_engine* h, bool want_grad) {
     a.lcodes = h->d_leafcodes.p;
     a.sched = static_cast<const SchedNode*>(h->d_sched.p);
     a.weights = static_cast<const double*>(h->d_weights.p);
+    a.plan = static_cast<const int32_t*>(h->d_plan.p);
+    a.max_J = h->max_J;
     if (h->inject == 1) h->inject = 0;
     CK(tc    ? launch_prune_tc(fmt, h->K, h->blocks, a, st)
+       : h->sweep == MCPHY_SWEEP_LEVEL ? launch_prune_level(f64, h->Kp, h->blocks, h->tpb, a, st)
        : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
              : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
     if (h->timing) CK(cudaEventRecord(h->ev[2], st));
@@ -798,7 +850,8 @@ int mcphy_destroy(mcphy_handle h) {
     drop_graphs(h);
     DevBuf* bufs[] = {&h->d_desc, &h->d_sched, &h->d_items, &h->d_queue, &h->d_steps,
                       &h->d_recs, &h->d_codes, &h->d_dense, &h->d_params, &h->d_blen, &h->d_pgrad,
-                      &h->d_pll, &h->d_part, &h->d_out, &h->d_post, &h->d_pre, &h->d_counter};
+                      &h->d_pll, &h->d_part, &h->d_out, &h->d_post, &h->d_pre, &h->d_counter,
+                      &h->d_plan};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     if (h->h_blen) cudaFreeHost(h->h_blen);
@@ -1100,6 +1153,23 @@ int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block)
     return MCPHY_OK;
 }
 
+int mcphy_set_sweep(mcphy_handle h, int sweep) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (sweep != MCPHY_SWEEP_AUTO && sweep != MCPHY_SWEEP_WALK && sweep != MCPHY_SWEEP_LEVEL)
+        return fail(h, MCPHY_ERR_ARG, "sweep must be MCPHY_SWEEP_AUTO, _WALK or _LEVEL");
+    h->sweep_req = sweep;
+    h->dirty |= DIRTY_LAYOUT;
+    return MCPHY_OK;
+}
+
+int mcphy_get_sweep(mcphy_handle h, int* sweep) {
+    if (!h || !sweep) return MCPHY_ERR_ARG;
+    int rc;
+    if ((rc = prepare(h))) return rc;
+    *sweep = h->sweep;
+    return MCPHY_OK;
+}
+
 int mcphy_debug_inject(mcphy_handle h, int kind) {
     if (!h) return MCPHY_ERR_ARG;
     if (kind < 0 || kind > 2) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
@@ -1126,43 +1196,59 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
         }
         return MCPHY_OK;
     }
-    std::vector<std::pair<int, int>> cand;
+    struct Cand {
+        int sweep, spt, tpb;
+    };
+    std::vector<Cand> cand;
     if (h->prec == MCPHY_PREC_F64)
-        cand = h->Kp <= 4 ? std::vector<std::pair<int, int>>{{1, 128}, {2, 128}, {1, 64}, {2, 64}}
-                          : std::vector<std::pair<int, int>>{{1, 128}, {1, 64}};
+        cand = h->Kp <= 4 ? std::vector<Cand>{{1, 1, 128}, {1, 2, 128}, {1, 1, 64}, {1, 2, 64}}
+                          : std::vector<Cand>{{1, 1, 128}, {1, 1, 64}};
     else if (h->Kp <= 4)
-        cand = {{4, 128}, {4, 64}, {2, 128}, {2, 64}, {4, 256}, {1, 128}};
+        cand = {{1, 4, 128}, {1, 4, 64}, {1, 2, 128}, {1, 2, 64}, {1, 4, 256}, {1, 1, 128}};
     else if (h->Kp <= 8)
-        cand = {{1, 128}, {2, 128}, {1, 64}, {2, 64}};
+        cand = {{1, 1, 128}, {1, 2, 128}, {1, 1, 64}, {1, 2, 64}};
     else
-        cand = {{1, 64}, {1, 128}, {1, 32}};
+        cand = {{1, 1, 64}, {1, 1, 128}, {1, 1, 32}};
+    // the level sweep where an item fits a CTA and the walk cannot fill the GPU
+    if (h->dirty & DIRTY_LAYOUT) {
+        int rc0 = prepare(h);
+        if (rc0) return rc0;
+    }
+    if (h->items_hint <= int64_t(8) * h->sm_count)
+        for (int t : {64, 128, 256})
+            if (level_fits(h, t)) cand.push_back({MCPHY_SWEEP_LEVEL, 1, t});
     const bool timing = h->timing, graph = h->use_graph;
     h->timing = true;
     h->use_graph = false;
     float best = 1e30f;
-    int bs = h->spt_req, bt = h->tpb_req;
+    int bw = h->sweep_req, bs = h->spt_req, bt = h->tpb_req;
     int rc = MCPHY_OK;
     std::vector<double> ll(h->M), g(1);
-    for (auto [spt, tpb] : cand) {
-        h->spt_req = spt;
-        h->tpb_req = tpb;
+    for (const Cand& c : cand) {
+        h->sweep_req = c.sweep;
+        h->spt_req = c.spt;
+        h->tpb_req = c.tpb;
         h->dirty |= DIRTY_LAYOUT;
         if ((rc = prepare(h))) break;
+        if (h->sweep != c.sweep) continue;   // did not fit
         if (g.size() < size_t(h->total_branch)) g.resize(h->total_branch);
         float t = 1e30f;
         for (int rep = 0; rep < 3 && rc == MCPHY_OK; ++rep) {
             rc = eval_host(h, ll.data(), g.data(), true);
-            if (rep > 0) t = std::min(t, h->ms[1]);
+            // the sweep and the reduction (item counts differ between launch shapes)
+            if (rep > 0) t = std::min(t, h->ms[1] + h->ms[2]);
         }
         if (rc) break;
         if (t < best) {
             best = t;
-            bs = spt;
-            bt = tpb;
+            bw = c.sweep;
+            bs = c.spt;
+            bt = c.tpb;
         }
     }
     h->timing = timing;
     h->use_graph = graph;
+    h->sweep_req = bw;
     h->spt_req = bs;
     h->tpb_req = bt;
     h->dirty |= DIRTY_LAYOUT;

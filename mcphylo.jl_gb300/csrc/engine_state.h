@@ -56,9 +56,12 @@ struct mcphy_engine {
     std::vector<Inst> inst;
     unsigned dirty = mcphy::DIRTY_LAYOUT | mcphy::DIRTY_DATA | mcphy::DIRTY_BLEN | mcphy::DIRTY_MODEL;
 
-    // launch shape
-    int spt_req = 0, tpb_req = 0;
-    int spt = 1, tpb = 256, blocks = 0;
+    // launch shape; sweep: MCPHY_SWEEP_WALK (a warp walks the whole tree) or
+    // MCPHY_SWEEP_LEVEL (a CTA's warps share the tree level by level)
+    int spt_req = 0, tpb_req = 0, sweep_req = 0;
+    int spt = 1, tpb = 256, blocks = 0, sweep = 1;
+    int32_t max_J_hint = 0;     // largest schedule, known before the layout (leaves - 1)
+    int64_t items_hint = 0;     // work items at 32-site blocks
 
     // layout
     std::vector<InstanceDesc> desc;
@@ -79,9 +82,11 @@ struct mcphy_engine {
     std::vector<int64_t> lc_off;      // per instance, into d_leafcodes
     bool any_dense = false;
     std::vector<SchedNode> sched_all;
+    std::vector<int32_t> plan_all;    // level plans, 2 J + 2 entries per instance
 
     DevBuf d_desc, d_sched, d_items, d_queue, d_steps, d_recs, d_codes, d_dense, d_params,
-        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter, d_leafcodes, d_weights;
+        d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter, d_leafcodes, d_weights,
+        d_plan;
     int n_split = 1;
 
     double* h_blen = nullptr;

@@ -23,6 +23,9 @@
 //      src/Likelihood/VectorizedFunctions.jl:2-213.)
 //   3. reduce: per (instance, branch) FP64 sums of the item partials in a fixed
 //      order (kernels_common.cu), so results are bit-reproducible run to run.
+// Small problems (too few site blocks to fill the GPU, trees small enough for one
+// CTA's shared memory) replace step 2 with the level-synchronous sweep of
+// kernels_level.cu, in which a CTA's warps share one tree level by level.
 //
 // Scaling: partials are rescaled by a power of two after every node (the
 // exponent of the per-site maximum) instead of by the maximum itself (by_max!).
@@ -87,7 +90,7 @@ struct PruneArgs {
     const int2* items;        // (instance, local item index)
     const int32_t* queue;     // order in which warps take items
     int32_t n_items;
-    int32_t* counter;         // [0] work counter, [1] error flag; zeroed before the launch
+    int32_t* counter;         // [0] work counter, [1] error flag; zeroed by the record build
     const unsigned char* recs;   // step records
     const void* codes;        // state bitmasks in schedule order, type by Kp:
                               // [block][step][operand][32*SPT] per instance
@@ -107,6 +110,8 @@ struct PruneArgs {
     const void* lcodes;       // leaf-major state codes [row][S_pad] (tensor-core path)
     const SchedNode* sched;   // schedule nodes (tensor-core path: sweep prologues)
     const double* weights;    // site-pattern weights per instance [S_pad], 0 past S
+    const int32_t* plan;      // level plans (level-synchronous sweep), per instance at plan_off
+    int32_t max_J;            // largest schedule (level-synchronous sweep: shared-memory layout)
 };
 
 // ---------------------------------------------------------------- tensor-core records
@@ -1044,6 +1049,15 @@ cudaError_t launch_prune_f64(int Kp, int spt, int blocks, int tpb, const PruneAr
                              cudaStream_t st);
 cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, int* blocks_per_sm);
 cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, int* blocks_per_sm);
+
+// Level-synchronous sweep for small trees (kernels_level.cu): a CTA of tpb threads
+// owns one 32-site work item at a time; its warps share the tree level by level.
+constexpr int kLevelSmemMax = 100 * 1024;   // per CTA: at least two CTAs per SM
+bool level_supported(int Kp);
+int level_smem_bytes(int Kp, int real_bytes, int max_J, int warps);
+cudaError_t launch_prune_level(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
+                               cudaStream_t st);
+cudaError_t occupancy_prune_level(bool f64, int Kp, int tpb, int max_J, int* blocks_per_sm);
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st);
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st);
 int reduce_launches(int n_split);   // kernels launch_reduce launches

@@ -1,0 +1,258 @@
+// Level-synchronous sweep for small trees (latency-bound problems).
+//
+// The tree-walk kernel gives every warp a whole tree: its time per evaluation is
+// the length of the schedule times the latency of one step, which is all there is
+// when a problem has too few site blocks to fill the GPU (a 32-taxon tree on 1000
+// sites is 32 warps).  Here a CTA owns 32 sites of one rate category (lane = site)
+// and its warps share the tree: the steps of one level (steps whose children all
+// lie on lower levels, from a host-built level plan) run on different warps at the
+// same time, with a CTA barrier between levels.  The critical path becomes the
+// tree's height instead of its number of internal nodes.
+//
+// Everything of a work item stays in shared memory: its step records (copied in
+// once), the post-order partial of every step and the pre-order partial of every
+// step.  The arithmetic is the tree-walk kernel's, step for step:
+//   post-order (FelsensteinFunction logL, LikelihoodCalculator_Node.jl:82-114):
+//     L_j = (P_0 L_op0) * (P_1 L_op1), power-of-two rescale, exponents summed per
+//     site; at the root log(pi . L) + e ln 2 (root_sum, VectorizedFunctions.jl:76-87);
+//   pre-order (gradient, LikelihoodCalculator_Node.jl:3-78), levels top down:
+//     pt_c = pb_j * D_sibling, gradient term (pt_c . dP_c L_c) / (pt_c . P_c L_c),
+//     pb_op_c = P_c^T pt_c rescaled.
+// Work items, per-item partial log-likelihoods and gradient partials are the
+// tree-walk kernel's (site block of 32), so the same reduction finishes them.
+// The kernel has no spin-waits: only CTA barriers, reached by every thread.
+#include <algorithm>
+
+#include "kernels.cuh"
+
+namespace mcphy {
+
+// Shared-memory bytes of one CTA for schedules of up to max_J steps.
+int level_smem_bytes(int kp, int real_bytes, int max_J, int warps) {
+    const int rb = rec_bytes(kp, real_bytes);
+    const int slot = 32 * kp * real_bytes;
+    return max_J * rb + 2 * max_J * slot + warps * 32 * 4 + 32 * real_bytes;
+}
+
+template <int KP, typename Real>
+__global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
+    constexpr int RB = rec_bytes(KP, sizeof(Real));
+    constexpr int SLOT = 32 * KP;   // Reals of one step's vector (32 sites)
+    constexpr double LN2 = 0.6931471805599453094;
+    using Code = typename CodeOf<KP>::type;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const int W = blockDim.x >> 5;
+    const int maxJ = a.max_J;
+    unsigned char* srec = smem;                                                  // maxJ x RB
+    Real* spost = reinterpret_cast<Real*>(smem + size_t(maxJ) * RB);           // maxJ x SLOT
+    Real* spre = spost + size_t(maxJ) * SLOT;                                  // maxJ x SLOT
+    uint32_t* sex = reinterpret_cast<uint32_t*>(spre + size_t(maxJ) * SLOT);   // W x 32
+    Real* sroot = reinterpret_cast<Real*>(sex + W * 32);                       // 32
+    const uint32_t allmask = (a.K >= 32) ? 0xffffffffu : ((1u << a.K) - 1u);
+    const int C = a.C;
+
+    for (int t = blockIdx.x; t < a.n_items; t += gridDim.x) {
+        const int item = __ldg(a.queue + t);
+        const int2 it = __ldg(a.items + item);
+        const InstanceDesc d = a.inst[it.x];
+        const int r = it.y / d.n_blocks;
+        const int blk = it.y - r * d.n_blocks;
+        const int site = blk * 32 + lane;
+        const bool valid = site < d.S;
+        const double wt = __ldg(a.weights + d.weight_off + site);
+        const int J = d.J;
+        const bool code_leaves = !d.dense;
+        const bool ambig = d.ambig != 0;
+        const Real* dense = reinterpret_cast<const Real*>(a.dense) + d.leaf_off;
+        const Code* codes = reinterpret_cast<const Code*>(a.lcodes) + d.lcode_off;
+        const double* pi_d = a.params + d.param_off + 2 * a.K * a.K + a.K + 1 + C;
+        const int32_t* plan = a.plan + d.plan_off;
+        const int H = __ldg(plan);
+        const int32_t* lstart = plan + 1;
+        const int32_t* order = plan + H + 2;
+
+        // the item's step records (rate r), 16 bytes per thread and pass
+        {
+            const int4* src = reinterpret_cast<const int4*>(a.recs + d.rec_off + size_t(r) * J * RB);
+            int4* dst = reinterpret_cast<int4*>(srec);
+            const int n = J * (RB / 16);
+            for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = __ldg(src + q);
+        }
+        __syncthreads();
+
+        // operand of a step when it is a leaf (leaf row -op-1), as the tree-walk
+        // kernel keeps it: the selected row index or bitmask in L[0][0]'s bits, or
+        // the dense partial
+        auto leaf = [&](int op, Real (&L)[1][KP]) {
+            const int64_t row = int64_t(-op - 1);
+            if (code_leaves) {
+                const uint32_t c = uint32_t(__ldg(codes + row * d.S_pad + site));
+                L[0][0] = u32_bits(ambig ? c : leaf_row<KP>(c, allmask), Real(0));
+            } else {
+                ld_vec_nc<KP>(dense + (row * d.S_pad + site) * KP, L[0]);
+            }
+        };
+        auto operand = [&](int op, Real (&L)[1][KP]) {
+            if (op >= 0) read_vec<KP, 1>(spost + size_t(op) * SLOT, lane, L);
+            else leaf(op, L);
+        };
+
+        // ---------------- post-order sweep, level by level
+        uint32_t eacc = 0u;
+        for (int l = 0; l < H; ++l) {
+            const int q1 = __ldg(lstart + l + 1);
+            for (int q = __ldg(lstart + l) + w; q < q1; q += W) {
+                const int j = __ldg(order + q);
+                const unsigned char* rj = srec + size_t(j) * RB;
+                int h[8];
+                rec_header(rj, h);
+                Real A[1][KP], B[1][KP], Da[1][KP], Db[1][KP];
+                operand(h[0], A);
+                operand(h[1], B);
+                down<KP, 1>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), Da);
+                down<KP, 1>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), Db);
+#pragma unroll
+                for (int k = 0; k < KP; ++k) Da[0][k] *= Db[0][k];
+                eacc += rescale<KP>(Da[0]);
+                if (j + 1 < J) {
+                    write_vec<KP, 1>(spost + size_t(j) * SLOT, lane, Da);
+                } else {
+                    Real lik = Real(0);
+#pragma unroll
+                    for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Da[0][k], lik);
+                    sroot[lane] = lik;
+                }
+            }
+            __syncthreads();
+        }
+        sex[w * 32 + lane] = eacc;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t tot = 0u;
+            for (int v = 0; v < W; ++v) tot += sex[v * 32 + lane];
+            const int ex = int(tot) - J * ExpBias<Real>::value;
+            const double v = log_site(sroot[lane]) + double(ex) * LN2;
+            double ll = valid ? wt * v : 0.0;
+            ll = warp_sum(ll);
+            if (lane == 0) a.pll[item] = ll;
+        }
+
+        // ---------------- pre-order sweep (gradient), levels top down
+        if (a.want_grad) {
+            Real* pg = reinterpret_cast<Real*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
+            for (int l = H - 1; l >= 0; --l) {
+                const int q1 = __ldg(lstart + l + 1);
+                for (int q = __ldg(lstart + l) + w; q < q1; q += W) {
+                    const int j = __ldg(order + q);
+                    const unsigned char* rj = srec + size_t(j) * RB;
+                    int h[8];
+                    rec_header(rj, h);
+                    Real pb[1][KP];
+                    if (j + 1 == J) {
+#pragma unroll
+                        for (int k = 0; k < KP; ++k) pb[0][k] = Real(__ldg(pi_d + k));
+                    } else {
+                        read_vec<KP, 1>(spre + size_t(j) * SLOT, lane, pb);
+                    }
+                    Real A[1][KP], B[1][KP], D[2][1][KP];
+                    operand(h[0], A);
+                    operand(h[1], B);
+                    down<KP, 1>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), D[0]);
+                    down<KP, 1>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        Real pt[1][KP];
+#pragma unroll
+                        for (int k = 0; k < KP; ++k) pt[0][k] = pb[0][k] * D[1 - c][0][k];
+                        if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
+                            Real dD[1][KP];
+                            if (c == 0)
+                                down<KP, 1>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
+                            else
+                                down<KP, 1>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 3), dD);
+                            Real num = Real(0), den = Real(0);
+#pragma unroll
+                            for (int k = 0; k < KP; ++k) {
+                                num = fma(pt[0][k], dD[0][k], num);
+                                den = fma(pt[0][k], D[c][0][k], den);
+                            }
+                            Real g = valid ? Real(wt) * ratio(num, den) : Real(0);
+                            g = warp_sum(g);
+                            if (lane == 0) pg[h[4 + c]] = g;
+                        }
+                        if (h[c] >= 0) {   // internal child: its pre-order partial
+                            Real pbc[1][KP];
+                            apply_tt<KP, 1>(rec_mat_ptr<KP, Real>(rj, 2 * c), pt, pbc);
+                            rescale<KP>(pbc[0]);
+                            write_vec<KP, 1>(spre + size_t(h[c]) * SLOT, lane, pbc);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();   // the next item restages the shared memory
+    }
+}
+
+// Dynamic shared memory allowed for each instantiation: raised to the largest size
+// any layout asked for and never lowered (handles of different sizes share it).
+// Raised by the layout's occupancy query and by the first, eager evaluation of a
+// layout, never inside a stream capture.
+template <int KP, typename Real>
+static cudaError_t allow_smem(int smem) {
+    static int allowed = 0;
+    if (smem <= allowed) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(prune_level_kernel<KP, Real>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) allowed = smem;
+    return e;
+}
+
+template <int KP, typename Real>
+static cudaError_t go_level(int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
+    const int smem = level_smem_bytes(KP, int(sizeof(Real)), a.max_J, tpb / 32);
+    cudaError_t e = allow_smem<KP, Real>(smem);
+    if (e != cudaSuccess) return e;
+    prune_level_kernel<KP, Real><<<blocks, tpb, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int KP, typename Real>
+static cudaError_t occ_level(int tpb, int max_J, int* bps) {
+    const int smem = level_smem_bytes(KP, int(sizeof(Real)), max_J, tpb / 32);
+    cudaError_t e = allow_smem<KP, Real>(smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_level_kernel<KP, Real>, tpb, smem);
+}
+
+bool level_supported(int kp) { return kp == 2 || kp == 4 || kp == 8; }
+
+cudaError_t launch_prune_level(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
+                               cudaStream_t st) {
+    switch (Kp * 2 + (f64 ? 1 : 0)) {
+        case 4: return go_level<2, float>(blocks, tpb, a, st);
+        case 5: return go_level<2, double>(blocks, tpb, a, st);
+        case 8: return go_level<4, float>(blocks, tpb, a, st);
+        case 9: return go_level<4, double>(blocks, tpb, a, st);
+        case 16: return go_level<8, float>(blocks, tpb, a, st);
+        case 17: return go_level<8, double>(blocks, tpb, a, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t occupancy_prune_level(bool f64, int Kp, int tpb, int max_J, int* bps) {
+    switch (Kp * 2 + (f64 ? 1 : 0)) {
+        case 4: return occ_level<2, float>(tpb, max_J, bps);
+        case 5: return occ_level<2, double>(tpb, max_J, bps);
+        case 8: return occ_level<4, float>(tpb, max_J, bps);
+        case 9: return occ_level<4, double>(tpb, max_J, bps);
+        case 16: return occ_level<8, float>(tpb, max_J, bps);
+        case 17: return occ_level<8, double>(tpb, max_J, bps);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace mcphy

@@ -58,7 +58,17 @@ struct alignas(16) InstanceDesc {
     int64_t grad_off;    // into the packed gradient output
     int64_t lcode_off;   // into the leaf-major code copy [row][S_pad] (code units)
     int64_t weight_off;  // into the site-pattern weights (S_pad doubles, 0 past S)
+    int64_t plan_off;    // into the level plans (int32 units, 2 J + 2 reserved per instance)
 };
+
+// Level plan of one schedule, for the level-synchronous sweep: step j's level is one
+// more than the highest level of its internal children (children that are leaves
+// count as level -1), so every step of a level depends only on lower levels.
+//   plan[0] = H (levels); plan[1 .. H+1] = start of each level in order[], then J;
+//   plan[H+2 ..] = order[J]: the steps sorted by level (stable: ascending j within
+//   a level).
+// Returns the number of int32 entries written (J + H + 2 <= 2 J + 2).
+int build_level_plan(const SchedNode* nodes, int32_t J, int32_t* plan);
 
 // FP64 model parameters of one instance, packed at param_off:
 //   U (K*K, column-major) | D (K) | Uinv (K*K) | mu (1) | rates (C) | pi (Kp)

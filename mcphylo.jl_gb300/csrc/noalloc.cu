@@ -139,7 +139,8 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     off += round_up(sizeof(double) * n_out);
     const size_t off_pgrad = off;
     off += round_up(rs * size_t(pgrad_elems));
-    const int wpb = h->tpb / 32;
+    // scratch columns per CTA: one per warp (tree walk), none (level sweep)
+    const int wpb = h->sweep == MCPHY_SWEEP_LEVEL ? 0 : h->tpb / 32;
     const size_t per_block_post = size_t(wpb) * size_t(h->warp_stride) * rs;
     const size_t per_block_pre = size_t(wpb) * size_t(h->pre_warp_stride) * rs;
     const size_t per_block = per_block_post + per_block_pre;
@@ -149,7 +150,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
                  std::to_string(kNoAllocScratchBytes) + " bytes";
         return MCPHY_ERR_ARG;
     }
-    int64_t blocks = int64_t((kNoAllocScratchBytes - off) / per_block);
+    int64_t blocks = per_block ? int64_t((kNoAllocScratchBytes - off) / per_block) : h->blocks;
     if (blocks > h->blocks) blocks = h->blocks;
     const size_t off_post = off;
     const size_t off_pre = off_post + round_up(size_t(blocks) * per_block_post);
@@ -198,8 +199,12 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     a.wait_limit = kWaitLimit;
     a.weights = static_cast<const double*>(h->d_weights.p);
     a.inject_timeout = 0;
-    NA_CK(f64 ? launch_prune_f64(h->Kp, h->spt, int(blocks), h->tpb, a, st)
-              : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, a, st));
+    a.lcodes = h->d_leafcodes.p;
+    a.plan = static_cast<const int32_t*>(h->d_plan.p);
+    a.max_J = h->max_J;
+    NA_CK(h->sweep == MCPHY_SWEEP_LEVEL ? launch_prune_level(f64, h->Kp, int(blocks), h->tpb, a, st)
+          : f64 ? launch_prune_f64(h->Kp, h->spt, int(blocks), h->tpb, a, st)
+                : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, a, st));
 
     ReduceArgs r{};
     r.inst = b.inst;

@@ -215,4 +215,26 @@ std::string build_schedule(int64_t N, const int64_t* parent,
     return std::string();
 }
 
+// Levels for the level-synchronous sweep: a counting sort of the steps by level.
+int build_level_plan(const SchedNode* nodes, int32_t J, int32_t* plan) {
+    std::vector<int32_t> level(J, 0);
+    int32_t H = 0;
+    for (int32_t j = 0; j < J; ++j) {   // post-order: children come first
+        int32_t l = 0;
+        for (int c = 0; c < 2; ++c)
+            if (nodes[j].op[c] >= 0) l = std::max(l, level[nodes[j].op[c]] + 1);
+        level[j] = l;
+        H = std::max(H, l + 1);
+    }
+    plan[0] = H;
+    int32_t* start = plan + 1;
+    int32_t* order = plan + H + 2;
+    std::fill(start, start + H + 1, 0);
+    for (int32_t j = 0; j < J; ++j) ++start[level[j] + 1];
+    for (int32_t l = 0; l < H; ++l) start[l + 1] += start[l];
+    std::vector<int32_t> fill(start, start + H);
+    for (int32_t j = 0; j < J; ++j) order[fill[level[j]]++] = j;
+    return J + H + 2;
+}
+
 }  // namespace mcphy

@@ -63,6 +63,8 @@ SIGNATURES = {
     "mcphy_synchronize": (c_int, [handle_t]),
     "mcphy_set_tiles": (c_int, [handle_t, c_int, c_int]),
     "mcphy_autotune": (c_int, [handle_t, P(c_int)]),
+    "mcphy_set_sweep": (c_int, [handle_t, c_int]),
+    "mcphy_get_sweep": (c_int, [handle_t, P(c_int)]),
     "mcphy_enable_graph": (c_int, [handle_t, c_int]),
     "mcphy_debug_inject": (c_int, [handle_t, c_int]),
     "mcphy_enable_timing": (c_int, [handle_t, c_int]),

@@ -140,6 +140,21 @@ class Engine:
         check(self._L.mcphy_set_tiles(self._h, sites_per_thread, threads_per_block), self._h,
               "set_tiles")
 
+    SWEEPS = {"auto": 0, "walk": 1, "level": 2}
+
+    def set_sweep(self, sweep: str = "auto") -> None:
+        """Sweep of the SIMT paths: "walk" (a warp walks the whole tree), "level"
+        (a CTA's warps share a small tree level by level) or "auto"."""
+        if sweep not in self.SWEEPS:
+            raise ValueError(f"sweep must be one of {sorted(self.SWEEPS)}")
+        check(self._L.mcphy_set_sweep(self._h, self.SWEEPS[sweep]), self._h, "set_sweep")
+
+    def sweep(self) -> str:
+        """The sweep the current layout uses (lays it out first if needed)."""
+        out = ctypes.c_int(0)
+        check(self._L.mcphy_get_sweep(self._h, ctypes.byref(out)), self._h, "get_sweep")
+        return {1: "walk", 2: "level"}[int(out.value)]
+
     def autotune(self):
         """Time the candidate launch shapes on the current problem; keep the fastest."""
         out = (ctypes.c_int * 2)()

@@ -76,10 +76,14 @@ def test_random_vs_oracle(built_lib, K, C, taxa, S, mf, model, precision):
     inst = random_instance(K, C, taxa, S, seed=K * 100 + C * 10 + taxa, multifurcate=mf,
                            model=model)
     llo, go = oracle(inst)
-    for spt in ((1, 2, 4) if K <= 4 else (1,)):
-        if precision == "f64" and spt == 4:
-            continue
+    shapes = [("walk", spt) for spt in ((1, 2, 4) if K <= 4 else (1,))
+              if not (precision == "f64" and spt == 4)]
+    if K <= 8:
+        shapes.append(("level", 0))
+    for sweep, spt in shapes:
         e = engine(inst, precision, spt)
+        e.set_sweep(sweep)
+        assert e.sweep() == sweep
         ll, g = e.logpdf_grad()
         assert e.logpdf() == pytest.approx(ll, rel=1e-15, abs=0)
         if precision == "f64":
@@ -91,8 +95,9 @@ def test_random_vs_oracle(built_lib, K, C, taxa, S, mf, model, precision):
         e.close()
 
 
+@pytest.mark.parametrize("sweep", ["walk", "level"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_dense_leaf_values(built_lib, precision):
+def test_dense_leaf_values(built_lib, precision, sweep):
     """Leaf partials that are not 0/1 (ambiguity weights) take the dense path."""
     inst = random_instance(4, 2, 15, 70, seed=7)
     x = inst.tensor()
@@ -103,10 +108,12 @@ def test_dense_leaf_values(built_lib, precision):
     t = O.tree_from_parent(inst.parent, inst.blen)
     llo, go = O.gradlogpdf(t, x, inst.pi, (inst.U, inst.D, inst.Uinv, inst.mu), inst.rates)
     e = mp.Engine(4, 2, precision)
+    e.set_sweep(sweep)
     e.set_tree(inst.parent, inst.blen)
     e.set_data(x, inst.leaf_nums)
     e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
     ll, g = e.logpdf_grad()
+    assert e.sweep() == sweep
     tol = F64_RTOL if precision == "f64" else F32_LL_RTOL
     assert abs(ll - llo) <= tol * abs(llo)
     if precision == "f64":
@@ -317,8 +324,9 @@ def test_full_size_gtr_gamma_f32_vs_f64(built_lib):
     assert abs(ll - llo) <= F64_RTOL * abs(llo)
 
 
+@pytest.mark.parametrize("sweep", ["walk", "level"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_partially_ambiguous_codes(built_lib, precision):
+def test_partially_ambiguous_codes(built_lib, precision, sweep):
     """0/1 leaf data where some cells allow two or three states (and one allows
     none) take the kernel's bitmask path; results match the oracle."""
     inst = random_instance(4, 2, 20, 90, seed=17)
@@ -330,7 +338,10 @@ def test_partially_ambiguous_codes(built_lib, precision):
     inst2 = simulate.Instance(inst.tree, inst.parent, inst.blen, inst.leaf_nums, codes, inst.U,
                               inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates)
     llo, go = oracle(inst2)
-    ll, g = engine(inst2, precision).logpdf_grad()
+    e = engine(inst2, precision)
+    e.set_sweep(sweep)
+    ll, g = e.logpdf_grad()
+    assert e.sweep() == sweep
     if precision == "f64":
         assert abs(ll - llo) <= F64_RTOL * abs(llo)
         assert_grad_close(g, go, F64_G_RTOL, F64_G_FLOOR)
@@ -344,6 +355,7 @@ def test_bounded_wait_timeout_is_reported_and_recoverable(built_lib):
     MCPHY_ERR_TIMEOUT instead of a hang; the context stays usable."""
     inst = random_instance(4, 2, 30, 300, seed=41)
     e = engine(inst, "f32")
+    e.set_sweep("walk")        # the sweep that stages its step records
     ll0, g0 = e.logpdf_grad()
     e.debug_inject(1)
     with pytest.raises(mp.MCPhyError) as ei:
@@ -414,6 +426,72 @@ def test_device_entry_graph_replay_matches_eager(built_lib, precision):
     llo, go = oracle(b)
     rtol = F64_RTOL if precision == "f64" else F32_LL_RTOL
     assert abs(runs[0][2][0][0] - llo) <= rtol * abs(llo)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_level_sweep_deep_chain_and_topology_moves(built_lib, precision):
+    """Level sweep on a 34-taxon caterpillar (one step per level, the longest chain
+    of barriers) and on a batch whose trees change topology on a live engine: the
+    level plans are rebuilt with the schedules; results match a fresh engine bit
+    for bit and the oracle within the path's tolerance."""
+    rng = np.random.default_rng(21)
+    cat = random_instance(4, 2, 0, 150, seed=22, tree=caterpillar(34, rng))
+    insts = [cat, random_instance(4, 2, 33, 97, seed=23, multifurcate=0.3),
+             random_instance(4, 2, 9, 40, seed=24)]
+    e = mp.Engine(4, 2, precision, n_instances=3)
+    e.set_sweep("level")
+    for i, b in enumerate(insts):
+        e.set_tree(b.parent, b.blen, i)
+        e.set_codes(b.codes, b.leaf_nums, i)
+        e.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, i)
+    e.enable_graph(True)
+    e.logpdf_grad()
+    assert e.sweep() == "level"
+    parents = [b.parent.copy() for b in insts]
+    tol = F64_RTOL if precision == "f64" else F32_LL_RTOL
+    for step in range(4):
+        i = step % 3
+        parents[i] = _nni(parents[i], rng)
+        e.set_tree(parents[i], insts[i].blen, i)
+        ll, g = e.logpdf_grad()
+        f = mp.Engine(4, 2, precision, n_instances=3)
+        f.set_sweep("level")
+        for k, b in enumerate(insts):
+            f.set_tree(parents[k], b.blen, k)
+            f.set_codes(b.codes, b.leaf_nums, k)
+            f.set_model(b.U, b.D, b.Uinv, b.mu, b.pi, b.rates, k)
+        llf, gf = f.logpdf_grad()
+        f.close()
+        assert np.array_equal(ll, llf) and np.array_equal(g, gf)
+        off = e.grad_offsets()
+        for k, b in enumerate(insts):
+            bk = simulate.Instance(T.from_parent(parents[k], b.blen), parents[k], b.blen,
+                                   b.leaf_nums, b.codes, b.U, b.D, b.Uinv, b.mu, b.pi, b.rates)
+            llo, go = oracle(bk)
+            assert abs(ll[k] - llo) <= tol * abs(llo)
+            if precision == "f64":
+                assert_grad_close(g[off[k]:off[k + 1]], go, F64_G_RTOL, F64_G_FLOOR)
+            else:
+                assert_grad_close(g[off[k]:off[k + 1]], go, F32_G_RTOL, F32_G_FLOOR)
+
+
+def test_automatic_sweep_choice(built_lib):
+    """Few 32-site blocks of a small tree: the level sweep; many site blocks, a tree
+    too large for one CTA, or 20 states: the tree walk."""
+    small = random_instance(2, 1, 32, 1000, seed=25, model="restriction")
+    assert engine(small, "f32").sweep() == "level"
+    assert engine(small, "f64").sweep() == "level"
+    many_sites = random_instance(4, 4, 32, 20000, seed=26)
+    assert engine(many_sites, "f32").sweep() == "walk"
+    big_tree = random_instance(4, 1, 400, 64, seed=27)
+    assert engine(big_tree, "f32").sweep() == "walk"
+    e = engine(big_tree, "f32")
+    e.set_sweep("level")                 # does not fit: falls back to the tree walk
+    assert e.sweep() == "walk"
+    k20 = random_instance(20, 2, 16, 40, seed=28)
+    assert engine(k20, "f32").sweep() == "walk"
+    walk_tiles = engine(small, "f32", spt=2)   # explicit tiles keep the tree walk
+    assert walk_tiles.sweep() == "walk"
 
 
 def test_autotune_keeps_results(built_lib):

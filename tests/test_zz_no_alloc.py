@@ -49,19 +49,26 @@ def _regular(L, _lib, h, blen, G):
     return ll[0], g
 
 
+@pytest.mark.parametrize("sweep", [1, 2])      # MCPHY_SWEEP_WALK, MCPHY_SWEEP_LEVEL
 @pytest.mark.parametrize("precision", [1, 0])   # MCPHY_PREC_F64, MCPHY_PREC_F32
-def test_noalloc_matches_regular_entry_point(built_lib, precision):
+def test_noalloc_matches_regular_entry_point(built_lib, precision, sweep):
     import torch
     from mcphylo_gb300 import _lib
     L = _lib.load()
-    inst = random_instance(4, 4, 60, 4000, seed=31, multifurcate=0.1)
+    if sweep == 1:
+        inst = random_instance(4, 4, 60, 4000, seed=31, multifurcate=0.1)
+    else:   # a tree whose items fit one CTA's shared memory
+        inst = random_instance(4, 4, 30, 500, seed=32, multifurcate=0.1)
     h = _handle(L, _lib, inst, precision)
+    assert L.mcphy_set_sweep(h, sweep) == 0
     try:
         G = inst.N - 1
         rng = np.random.default_rng(5)
         blens = [inst.blen * rng.uniform(0.7, 1.3, size=G) for _ in range(2)]
         # a regular call first: it uploads the tree, data and model (and allocates)
         _regular(L, _lib, h, inst.blen.copy(), G)
+        got = ctypes.c_int(0)
+        assert L.mcphy_get_sweep(h, ctypes.byref(got)) == 0 and got.value == sweep
         d_ll = torch.zeros(1, dtype=torch.float64, device="cuda")
         d_g = torch.zeros(G, dtype=torch.float64, device="cuda")
         for blen in blens:                       # two allocation-free calls in a row
