@@ -4,7 +4,7 @@ import pytest
 
 from conftest import load_alignment
 from gpu_cases import (F32_G_FLOOR, F32_G_RTOL, F32_LL_RTOL, F64_G_FLOOR, F64_G_RTOL, F64_RTOL,
-                       assert_grad_close, caterpillar, engine, oracle, oracle_ll,
+                       assert_grad_close, caterpillar, engine, level_fits, oracle, oracle_ll,
                        random_instance)
 
 import mcphylo_gb300 as mp
@@ -78,7 +78,7 @@ def test_random_vs_oracle(built_lib, K, C, taxa, S, mf, model, precision):
     llo, go = oracle(inst)
     shapes = [("walk", spt) for spt in ((1, 2, 4) if K <= 4 else (1,))
               if not (precision == "f64" and spt == 4)]
-    if K <= 8:
+    if level_fits(K, len(inst.leaf_nums), precision):
         shapes.append(("level", 0))
     for sweep, spt in shapes:
         e = engine(inst, precision, spt)
