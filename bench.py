@@ -73,11 +73,13 @@ def make_workload(name, workers):
     return insts, cfg
 
 
-def make_engine(insts, precision, tiles=None):
+def make_engine(insts, precision, tiles=None, sweep="auto"):
     import mcphylo_gb300 as mp
     e = mp.Engine(insts[0].K, len(insts[0].rates), precision, n_instances=len(insts))
     if tiles:
         e.set_tiles(*tiles)
+    if precision in ("f32", "f64"):
+        e.set_sweep(sweep)
     for i, b in enumerate(insts):
         e.set_tree(b.parent, b.blen, i)
         e.set_codes(b.codes, b.leaf_nums, i)
@@ -129,6 +131,23 @@ def algorithmic_bytes(insts, spt, real_bytes, grad=True):
         if grad:
             total += 2 * lanes * (info["internal"] - 1) * Kp * real_bytes
             total += C * blocks * (b.N - 1) * real_bytes
+    return total
+
+
+def level_algorithmic_bytes(insts, real_bytes, grad=True):
+    """Bytes the level-synchronous sweep must move per evaluation: its partials stay
+    in shared memory, so the leaf state codes read once, the step records read once
+    per (instance, rate) and the per-item gradient partials written once."""
+    K = insts[0].K
+    Kp = 2 if K <= 2 else 4 if K <= 4 else 8
+    rec = 48 + 4 * (Kp + 1) * Kp * real_bytes
+    total = 0
+    for b in insts:
+        C = len(b.rates)
+        J = len(b.leaf_nums) - 1
+        total += len(b.leaf_nums) * b.S * 1 + C * J * rec
+        if grad:
+            total += C * (-(-b.S // 32)) * (b.N - 1) * real_bytes
     return total
 
 
@@ -424,15 +443,17 @@ def run_gpu(args, rank, world):
     tc_path = prec in ("tf32", "bf16")
     if tc_path and insts[0].K < 9:
         raise SystemExit("--precision tf32/bf16 is the dense-state path (K >= 9)")
-    if args.tiles == "auto":
-        # the library's autotuner: times each launch shape on this problem
+    if args.tiles == "auto" and args.sweep == "auto":
+        # the library's autotuner: times each sweep and launch shape on this problem
         e = make_engine(insts, prec)
         tiles = e.autotune()
         tune = {"chosen_by": "mcphy_autotune"}
     else:
-        tiles = tuple(int(x) for x in args.tiles.split("x"))
-        tune = {}
-        e = make_engine(insts, prec, tiles)
+        tiles = None if args.tiles == "auto" else tuple(int(x) for x in args.tiles.split("x"))
+        tune = {"chosen_by": "command line"}
+        e = make_engine(insts, prec, tiles, args.sweep)
+        tiles = tiles or (1, 128)
+    sweep = e.sweep() if not tc_path else "tensor-core"
     M = len(insts)
     off = e.grad_offsets()
     G = int(off[-1])
@@ -596,12 +617,17 @@ def run_gpu(args, rank, world):
         e32.close()
 
     real_b = 4
+    K0 = insts[0].K
+    kp = 2 if K0 <= 2 else 4 if K0 <= 4 else 8 if K0 <= 8 else 20 if K0 <= 20 else 32
     if tc_path:
         alg = tc_algorithmic_bytes(insts, args.mode == "grad", prec == "bf16")
-        kname = "prune_tc_kernel<%d,%s>" % ((insts[0].K + 7) // 8 * 8, prec)
+        kname = "prune_tc_kernel<%d,%s>" % ((K0 + 7) // 8 * 8, prec)
+    elif sweep == "level":
+        alg = level_algorithmic_bytes(insts, real_b, args.mode == "grad")
+        kname = "prune_level_kernel<%d,float>" % kp
     else:
         alg = algorithmic_bytes(insts, tiles[0], real_b, args.mode == "grad")
-        kname = "prune_kernel<4,float,%d>" % tiles[0]
+        kname = "prune_kernel<%d,float,%d>" % (kp, tiles[0])
     pr = statistics.mean(prune_ms)
     achieved = alg / (pr / 1e3) / 1e9
     # DRAM bytes of one prune launch from the committed ncu capture: bytes per unit
@@ -651,6 +677,7 @@ def run_gpu(args, rank, world):
            "vs_baseline": None, "dtype": prec,
            "data": "synthetic (seeded simulation down Yule trees)",
            "config": dict(cfg, tiles={"sites_per_thread": tiles[0], "threads_per_block": tiles[1]},
+                          sweep=sweep,
                           l2="flushed between steps (512 MB write, outside the timed events)",
                           parallelism="replicas" if world > 1 else "single GPU"),
            "clocks": clocks, "e2e": e2e,
@@ -676,6 +703,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-hky-g4")
     ap.add_argument("--tiles", default="auto", help="auto or SPTxTPB, e.g. 2x256")
+    ap.add_argument("--sweep", default="auto", choices=["auto", "walk", "level"],
+                    help="SIMT sweep; auto with --tiles auto runs the library's autotuner")
     ap.add_argument("--mode", default="grad", choices=["grad", "logl", "nuts"],
                     help="grad: logL + gradient (the headline metric); logl: logL only; "
                          "nuts: PNUTS ESS/s on a single-tree workload")

@@ -10,7 +10,8 @@ namespace mcphy {
 // Block (bx, i, z) sums the items of instance i in split z (a contiguous item
 // range) for 32 branches; thread (tx, ty) takes every RY-th item of the range,
 // then the RY partial sums are added in ty order.  The last x-block does the
-// log-likelihood partials.  Pass 2 adds the n_split sums in z order.
+// log-likelihood partials (a shuffle tree per warp, then the warp sums in order).
+// Pass 2 adds the n_split sums in z order; with one split, pass 1 writes the results.
 template <typename Real>
 __global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
     __shared__ double red[RY][33];
@@ -27,12 +28,13 @@ __global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
         const int tid = ty * 32 + tx;
         double acc = 0.0;
         for (int64_t q = q0 + tid; q < q1; q += 32 * RY) acc += a.pll[d.item_off + q];
-        red[ty][tx] = acc;
+        // a fixed tree: each warp by shuffles, then the RY warp sums in order
+        acc = warp_sum(acc);
+        if (tx == 0) red[ty][0] = acc;
         __syncthreads();
         if (tid == 0) {
             double s = 0.0;
-            for (int y = 0; y < RY; ++y)
-                for (int x = 0; x < 32; ++x) s += red[y][x];
+            for (int y = 0; y < RY; ++y) s += red[y][0];
             part[i] = s;
         }
         return;
