@@ -9,9 +9,10 @@
 // same time, with a CTA barrier between levels.  The critical path becomes the
 // tree's height instead of its number of internal nodes.
 //
-// Everything of a work item stays in shared memory: its step records (copied in
-// once), the post-order partial of every step and the pre-order partial of every
-// step.  The arithmetic is the tree-walk kernel's, step for step:
+// Everything of a work item stays in shared memory: its step records, level plan
+// and leaf state codes (copied in once per item), the post-order partial of every
+// step and the pre-order partial of every step; no global load sits on the chain
+// of dependent steps.  The arithmetic is the tree-walk kernel's, step for step:
 //   post-order (FelsensteinFunction logL, LikelihoodCalculator_Node.jl:82-114):
 //     L_j = (P_0 L_op0) * (P_1 L_op1), power-of-two rescale, exponents summed per
 //     site; at the root log(pi . L) + e ln 2 (root_sum, VectorizedFunctions.jl:76-87);
@@ -27,15 +28,30 @@
 
 namespace mcphy {
 
-// Shared-memory bytes of one CTA for schedules of up to max_J steps.
+// Shared-memory layout of one CTA for schedules of up to max_J steps (bytes, every
+// part a multiple of 16): records | post partials | pre partials | exponent sums
+// (per warp) | root likelihoods | level plan | leaf codes.
+struct LevelSmem {
+    int rec, post, pre, ex, root, plan, code, total;
+    __host__ __device__ LevelSmem(int kp, int real_bytes, int max_J, int warps) {
+        const int slot = 32 * kp * real_bytes;
+        rec = 0;
+        post = rec + max_J * rec_bytes(kp, real_bytes);
+        pre = post + max_J * slot;
+        ex = pre + max_J * slot;
+        root = ex + warps * 32 * 4;
+        plan = root + 32 * real_bytes;
+        code = plan + (4 * (2 * max_J + 2) + 15) / 16 * 16;
+        total = code + (max_J + 1) * 32 * code_bytes(kp);
+    }
+};
+
 int level_smem_bytes(int kp, int real_bytes, int max_J, int warps) {
-    const int rb = rec_bytes(kp, real_bytes);
-    const int slot = 32 * kp * real_bytes;
-    return max_J * rb + 2 * max_J * slot + warps * 32 * 4 + 32 * real_bytes;
+    return LevelSmem(kp, real_bytes, max_J, warps).total;
 }
 
 template <int KP, typename Real>
-__global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
+__global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) {
     constexpr int RB = rec_bytes(KP, sizeof(Real));
     constexpr int SLOT = 32 * KP;   // Reals of one step's vector (32 sites)
     constexpr double LN2 = 0.6931471805599453094;
@@ -44,12 +60,14 @@ __global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int W = blockDim.x >> 5;
-    const int maxJ = a.max_J;
-    unsigned char* srec = smem;                                                  // maxJ x RB
-    Real* spost = reinterpret_cast<Real*>(smem + size_t(maxJ) * RB);           // maxJ x SLOT
-    Real* spre = spost + size_t(maxJ) * SLOT;                                  // maxJ x SLOT
-    uint32_t* sex = reinterpret_cast<uint32_t*>(spre + size_t(maxJ) * SLOT);   // W x 32
-    Real* sroot = reinterpret_cast<Real*>(sex + W * 32);                       // 32
+    const LevelSmem lay(KP, int(sizeof(Real)), a.max_J, W);
+    unsigned char* srec = smem + lay.rec;
+    Real* spost = reinterpret_cast<Real*>(smem + lay.post);
+    Real* spre = reinterpret_cast<Real*>(smem + lay.pre);
+    uint32_t* sex = reinterpret_cast<uint32_t*>(smem + lay.ex);
+    Real* sroot = reinterpret_cast<Real*>(smem + lay.root);
+    int32_t* splan = reinterpret_cast<int32_t*>(smem + lay.plan);
+    Code* scode = reinterpret_cast<Code*>(smem + lay.code);
     const uint32_t allmask = (a.K >= 32) ? 0xffffffffu : ((1u << a.K) - 1u);
     const int C = a.C;
 
@@ -66,21 +84,32 @@ __global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
         const bool code_leaves = !d.dense;
         const bool ambig = d.ambig != 0;
         const Real* dense = reinterpret_cast<const Real*>(a.dense) + d.leaf_off;
-        const Code* codes = reinterpret_cast<const Code*>(a.lcodes) + d.lcode_off;
         const double* pi_d = a.params + d.param_off + 2 * a.K * a.K + a.K + 1 + C;
-        const int32_t* plan = a.plan + d.plan_off;
-        const int H = __ldg(plan);
-        const int32_t* lstart = plan + 1;
-        const int32_t* order = plan + H + 2;
 
-        // the item's step records (rate r), 16 bytes per thread and pass
+        // the item's step records (rate r), level plan and leaf codes (its 32 sites
+        // of every leaf row), 16 bytes per thread and pass
         {
             const int4* src = reinterpret_cast<const int4*>(a.recs + d.rec_off + size_t(r) * J * RB);
             int4* dst = reinterpret_cast<int4*>(srec);
             const int n = J * (RB / 16);
             for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = __ldg(src + q);
+            const int32_t* gplan = a.plan + d.plan_off;
+            for (int q = threadIdx.x; q < 2 * J + 2; q += blockDim.x) splan[q] = __ldg(gplan + q);
+            if (code_leaves) {
+                // row l: sites blk*32 .. +32 of the leaf-major copy, 32 * sizeof(Code) bytes
+                constexpr int V = 32 * int(sizeof(Code)) / 16;   // int4 per row
+                const Code* gcode = reinterpret_cast<const Code*>(a.lcodes) + d.lcode_off + blk * 32;
+                for (int q = threadIdx.x; q < d.n_leaf * V; q += blockDim.x) {
+                    const int l = q / V;
+                    reinterpret_cast<int4*>(scode)[q] =
+                        __ldg(reinterpret_cast<const int4*>(gcode + int64_t(l) * d.S_pad) + (q - l * V));
+                }
+            }
         }
         __syncthreads();
+        const int H = splan[0];
+        const int32_t* lstart = splan + 1;
+        const int32_t* order = splan + H + 2;
 
         // operand of a step when it is a leaf (leaf row -op-1), as the tree-walk
         // kernel keeps it: the selected row index or bitmask in L[0][0]'s bits, or
@@ -88,7 +117,7 @@ __global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
         auto leaf = [&](int op, Real (&L)[1][KP]) {
             const int64_t row = int64_t(-op - 1);
             if (code_leaves) {
-                const uint32_t c = uint32_t(__ldg(codes + row * d.S_pad + site));
+                const uint32_t c = uint32_t(scode[row * 32 + lane]);
                 L[0][0] = u32_bits(ambig ? c : leaf_row<KP>(c, allmask), Real(0));
             } else {
                 ld_vec_nc<KP>(dense + (row * d.S_pad + site) * KP, L[0]);
@@ -102,9 +131,9 @@ __global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
         // ---------------- post-order sweep, level by level
         uint32_t eacc = 0u;
         for (int l = 0; l < H; ++l) {
-            const int q1 = __ldg(lstart + l + 1);
-            for (int q = __ldg(lstart + l) + w; q < q1; q += W) {
-                const int j = __ldg(order + q);
+            const int q1 = lstart[l + 1];
+            for (int q = lstart[l] + w; q < q1; q += W) {
+                const int j = order[q];
                 const unsigned char* rj = srec + size_t(j) * RB;
                 int h[8];
                 rec_header(rj, h);
@@ -143,9 +172,9 @@ __global__ void __launch_bounds__(256) prune_level_kernel(const PruneArgs a) {
         if (a.want_grad) {
             Real* pg = reinterpret_cast<Real*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
             for (int l = H - 1; l >= 0; --l) {
-                const int q1 = __ldg(lstart + l + 1);
-                for (int q = __ldg(lstart + l) + w; q < q1; q += W) {
-                    const int j = __ldg(order + q);
+                const int q1 = lstart[l + 1];
+                for (int q = lstart[l] + w; q < q1; q += W) {
+                    const int j = order[q];
                     const unsigned char* rj = srec + size_t(j) * RB;
                     int h[8];
                     rec_header(rj, h);

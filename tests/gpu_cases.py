@@ -72,14 +72,16 @@ def oracle_ll(inst, blen=None):
 def level_fits(K, n_leaves, precision, warps=4):
     """Whether an item of the level-synchronous sweep fits one CTA's shared memory
     (the library's rule: records, post- and pre-order partials of every step of a
-    32-site block, at most 100 KB)."""
+    32-site block, level plan and leaf codes, at most 100 KB)."""
     kp = 2 if K <= 2 else 4 if K <= 4 else 8 if K <= 8 else 0
     if not kp:
         return False
     b = 8 if precision == "f64" else 4
     J = n_leaves - 1
     rec = 48 + 4 * (kp + 1) * kp * b
-    return J * rec + 2 * J * 32 * kp * b + warps * 32 * 4 + 32 * b <= 100 * 1024
+    plan = (4 * (2 * J + 2) + 15) // 16 * 16
+    total = J * rec + 2 * J * 32 * kp * b + warps * 32 * 4 + 32 * b + plan + (J + 1) * 32
+    return total <= 100 * 1024
 
 
 def engine(inst, precision, spt=0, dense=False):
