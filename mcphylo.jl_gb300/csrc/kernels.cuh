@@ -730,11 +730,12 @@ prune_kernel(const PruneArgs a) {
         const Real* dense = reinterpret_cast<const Real*>(a.dense) + d.leaf_off;
 
         bool valid[SPT];
-        double wt[SPT];            // site-pattern weight (each site's log and gradient terms)
+        Real wtr[SPT];             // site-pattern weight of the gradient terms (the
+                                   // log-likelihood reloads it in FP64 at the root)
 #pragma unroll
         for (int u = 0; u < SPT; ++u) {
             valid[u] = (site0 + 32 * u) < d.S;
-            wt[u] = __ldg(a.weights + d.weight_off + site0 + 32 * u);
+            wtr[u] = Real(__ldg(a.weights + d.weight_off + site0 + 32 * u));
         }
 
         // operand c of step j when it is a leaf, into L
@@ -803,7 +804,8 @@ prune_kernel(const PruneArgs a) {
                     for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Da[u][k], lik);
                     const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
                     const double v = log_site(lik) + double(ex) * LN2;
-                    ll_lane += valid[u] ? wt[u] * v : 0.0;
+                    const double w = __ldg(a.weights + d.weight_off + site0 + 32 * u);
+                    ll_lane += valid[u] ? w * v : 0.0;
                 }
             }
             // chunk finished: refill its buffers with the chunk after next
@@ -868,6 +870,7 @@ prune_kernel(const PruneArgs a) {
             down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), D[0]);
             down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
             Real Npb[SPT][KP];
+            Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 // pre-order partial at the top of branch c: mother's pre times the
@@ -904,10 +907,9 @@ prune_kernel(const PruneArgs a) {
                                 den = fma(pt[u][k], D[c][u][k], den);
                             }
                         }
-                        g += valid[u] ? Real(wt[u]) * ratio(num, den) : Real(0);
+                        g += valid[u] ? wtr[u] * ratio(num, den) : Real(0);
                     }
-                    g = warp_sum(g);
-                    if (lane == 0) pg[h[4 + c]] = g;
+                    gsum[c] = g;
                 }
                 if (h[c] >= 0) {
                     Real pbc[SPT][KP];
@@ -917,6 +919,18 @@ prune_kernel(const PruneArgs a) {
                     if (c == 1) copy_part(Npb, pbc);                             // step j-1
                     else write_vec<KP, SPT>(stack_ptr(h[2]), lane, pbc);
                 }
+            }
+            if (h[4] >= 0 || h[5] >= 0) {
+                // both children's warp sums in one shuffle tree: lanes 0-15 add child
+                // 0's terms, lanes 16-31 child 1's (the same pairs, in the same order,
+                // as a warp_sum of each)
+                const bool hi = (lane & 16) != 0;
+                Real v = hi ? gsum[1] : gsum[0];
+                v += __shfl_xor_sync(0xffffffffu, hi ? gsum[0] : gsum[1], 16);
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0 && h[4] >= 0) pg[h[4]] = v;
+                if (lane == 16 && h[5] >= 0) pg[h[5]] = v;
             }
             if (h[1] >= 0) copy_part(pb, Npb);
             // chunk finished (descending): refill its buffers two chunks below
