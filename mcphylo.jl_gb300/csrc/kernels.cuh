@@ -730,12 +730,14 @@ prune_kernel(const PruneArgs a) {
         const Real* dense = reinterpret_cast<const Real*>(a.dense) + d.leaf_off;
 
         bool valid[SPT];
-        Real wtr[SPT];             // site-pattern weight of the gradient terms (the
-                                   // log-likelihood reloads it in FP64 at the root)
+        // site-pattern weight of the gradient terms, 0 past the last site (padding
+        // sites allow every state, so their terms are finite); the log-likelihood
+        // reloads it in FP64 at the root
+        Real wtr[SPT];
 #pragma unroll
         for (int u = 0; u < SPT; ++u) {
             valid[u] = (site0 + 32 * u) < d.S;
-            wtr[u] = Real(__ldg(a.weights + d.weight_off + site0 + 32 * u));
+            wtr[u] = valid[u] ? Real(__ldg(a.weights + d.weight_off + site0 + 32 * u)) : Real(0);
         }
 
         // operand c of step j when it is a leaf, into L
@@ -907,7 +909,7 @@ prune_kernel(const PruneArgs a) {
                                 den = fma(pt[u][k], D[c][u][k], den);
                             }
                         }
-                        g += valid[u] ? wtr[u] * ratio(num, den) : Real(0);
+                        g = fma(wtr[u], ratio(num, den), g);
                     }
                     gsum[c] = g;
                 }
