@@ -397,6 +397,10 @@ int gather_instance(mcphy_engine* h, int64_t i) {
     g.n_blocks = d.n_blocks;
     g.slot_words = 32 * h->spt * cb / 4;
     g.row_words = int64_t(d.S_pad) * cb / 4;
+    g.code_bytes = cb;
+    g.rows = d.ambig ? 0 : 1;
+    g.kp = h->Kp;
+    g.allmask = (h->K == 32) ? 0xffffffffu : ((1u << h->K) - 1u);
     CK(launch_gather_codes(g, h->stream));
     return MCPHY_OK;
 }

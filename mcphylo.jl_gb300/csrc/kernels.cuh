@@ -92,8 +92,9 @@ struct PruneArgs {
     int32_t n_items;
     int32_t* counter;         // [0] work counter, [1] error flag; zeroed by the record build
     const unsigned char* recs;   // step records
-    const void* codes;        // state bitmasks in schedule order, type by Kp:
-                              // [block][step][operand][32*SPT] per instance
+    const void* codes;        // leaf codes in schedule order, type by Kp: row indices,
+                              // or bitmasks for instances with partially ambiguous
+                              // codes; [block][step][operand][32*SPT] per instance
     const void* dense;        // Real [leaf_row][S_pad][Kp]
     const double* params;     // per-instance FP64 parameters
     void* post;               // Real scratch, [warp][node slot][SPT][32][Kp]
@@ -627,16 +628,15 @@ __device__ __forceinline__ void write_vec(Real* v, int lane, const Real (&L)[SPT
 #pragma unroll
     for (int u = 0; u < SPT; ++u) st_vec<KP>(v + (u * 32 + lane) * KP, L[u]);
 }
-// Leaf codes of the warp's sites in a ring slot -> row indices (or bitmasks).
+// Leaf codes of the warp's sites in a ring slot.  The schedule-ordered copy holds
+// row indices already (0..K-1 one state, KP every state) for instances without
+// partially ambiguous codes, else the raw bitmasks (gather_codes_kernel).
 template <int KP, int SPT, typename Real>
-__device__ __forceinline__ void read_codes(const unsigned char* p, int lane, bool ambig,
-                                           uint32_t allmask, Real (&L)[SPT][KP]) {
+__device__ __forceinline__ void read_codes(const unsigned char* p, int lane, Real (&L)[SPT][KP]) {
     using Code = typename CodeOf<KP>::type;
 #pragma unroll
-    for (int u = 0; u < SPT; ++u) {
-        const uint32_t c = uint32_t(reinterpret_cast<const Code*>(p)[u * 32 + lane]);
-        L[u][0] = u32_bits(ambig ? c : leaf_row<KP>(c, allmask), Real(0));
-    }
+    for (int u = 0; u < SPT; ++u)
+        L[u][0] = u32_bits(uint32_t(reinterpret_cast<const Code*>(p)[u * 32 + lane]), Real(0));
 }
 
 // Down vectors (or dD = dP L) of an operand through one table T of a child.
@@ -658,6 +658,12 @@ __device__ __forceinline__ void down(const Real (&L)[SPT][KP], bool code_leaf, b
 // inside the 1e-4 per-entry gradient tolerance; FP64: IEEE division.
 __device__ __forceinline__ float ratio(float n, float d) { return __fdividef(n, d); }
 __device__ __forceinline__ double ratio(double n, double d) { return n / d; }
+// The same with a denominator shared by two ratios: FP32 keeps its reciprocal,
+// FP64 the denominator itself (IEEE division).
+__device__ __forceinline__ float den_prep(float d) { return __fdividef(1.0f, d); }
+__device__ __forceinline__ double den_prep(double d) { return d; }
+__device__ __forceinline__ float den_apply(float n, float r) { return n * r; }
+__device__ __forceinline__ double den_apply(double n, double d) { return n / d; }
 
 // Site log-likelihood of the root sum, in FP64: with lazy rescaling the root sum can
 // lie far below 1, where an FP32 logarithm would lose absolute accuracy.
@@ -696,7 +702,6 @@ prune_kernel(const PruneArgs a) {
     Real* post = reinterpret_cast<Real*>(a.post) + gw * a.warp_stride;
     Real* gstack = reinterpret_cast<Real*>(a.pre) + gw * a.pre_warp_stride;
     const int C = a.C;
-    const uint32_t allmask = (a.K >= 32) ? 0xffffffffu : ((1u << a.K) - 1u);
     constexpr double LN2 = 0.6931471805599453094;
 
     unsigned char* wbase = smem + size_t(wib) * warp_smem_bytes(KP, SPT, int(sizeof(Real)));
@@ -743,7 +748,7 @@ prune_kernel(const PruneArgs a) {
         // operand c of step j when it is a leaf, into L
         auto leaf = [&](int j, int c, int op, Real (&L)[SPT][KP]) {
             if (code_leaves) {
-                read_codes<KP, SPT>(st.tip(j, c), lane, ambig, allmask, L);
+                read_codes<KP, SPT>(st.tip(j, c), lane, L);
             } else {
                 const int64_t row = int64_t(-op - 1);
 #pragma unroll
@@ -873,6 +878,10 @@ prune_kernel(const PruneArgs a) {
             down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
             Real Npb[SPT][KP];
             Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
+            // the gradient ratio's denominator pt_c . D_c = sum_k pb_k D0_k D1_k is the
+            // same for both children: computed once, with child 0's pt
+            Real den[SPT];
+            const bool any_grad = h[4] >= 0 || h[5] >= 0;
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 // pre-order partial at the top of branch c: mother's pre times the
@@ -890,6 +899,21 @@ prune_kernel(const PruneArgs a) {
                         for (int k = 0; k < KP; ++k) pt[u][k] = pb[u][k] * D[1 - c][u][k];
                     }
                 }
+                if (c == 0 && any_grad) {
+#pragma unroll
+                    for (int u = 0; u < SPT; ++u) {
+                        Real s0 = Real(0), s1 = Real(0);
+                        if constexpr (Pairs<Real, KP>::value) {
+#pragma unroll
+                            for (int k = 0; k < KP; k += 2)
+                                fma2(pt[u][k], pt[u][k + 1], D[0][u][k], D[0][u][k + 1], s0, s1);
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < KP; ++k) s0 = fma(pt[u][k], D[0][u][k], s0);
+                        }
+                        den[u] = den_prep(s0 + s1);
+                    }
+                }
                 if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
                     if (c == 0) down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
@@ -897,19 +921,16 @@ prune_kernel(const PruneArgs a) {
                     Real g = Real(0);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
-                        Real num = Real(0), den = Real(0);
+                        Real n0 = Real(0), n1 = Real(0);
                         if constexpr (Pairs<Real, KP>::value) {
 #pragma unroll
-                            for (int k = 0; k < KP; ++k)
-                                fma2(pt[u][k], pt[u][k], dD[u][k], D[c][u][k], num, den);
+                            for (int k = 0; k < KP; k += 2)
+                                fma2(pt[u][k], pt[u][k + 1], dD[u][k], dD[u][k + 1], n0, n1);
                         } else {
 #pragma unroll
-                            for (int k = 0; k < KP; ++k) {
-                                num = fma(pt[u][k], dD[u][k], num);
-                                den = fma(pt[u][k], D[c][u][k], den);
-                            }
+                            for (int k = 0; k < KP; ++k) n0 = fma(pt[u][k], dD[u][k], n0);
                         }
-                        g = fma(wtr[u], ratio(num, den), g);
+                        g = fma(wtr[u], den_apply(n0 + n1, den[u]), g);
                     }
                     gsum[c] = g;
                 }
@@ -1093,6 +1114,11 @@ struct GatherArgs {
     int32_t n_blocks;
     int32_t slot_words;       // site block x code bytes / 4
     int64_t row_words;        // S_pad x code bytes / 4
+    int32_t code_bytes;       // 1 (K <= 8) or 4
+    int32_t rows;             // 1: store row indices (the instance has no partially
+                              // ambiguous codes): one state s -> s, every state -> Kp
+    int32_t kp;
+    uint32_t allmask;
 };
 cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st);
 
