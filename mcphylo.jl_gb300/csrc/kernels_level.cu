@@ -96,13 +96,21 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
             const int32_t* gplan = a.plan + d.plan_off;
             for (int q = threadIdx.x; q < 2 * J + 2; q += blockDim.x) splan[q] = __ldg(gplan + q);
             if (code_leaves) {
-                // row l: sites blk*32 .. +32 of the leaf-major copy, 32 * sizeof(Code) bytes
+                // row l: sites blk*32 .. +32 of the leaf-major copy, 32 * sizeof(Code) bytes,
+                // stored as the row of the record's tables each code selects (the state's
+                // index, KP for every state) unless the instance has partially ambiguous codes
                 constexpr int V = 32 * int(sizeof(Code)) / 16;   // int4 per row
                 const Code* gcode = reinterpret_cast<const Code*>(a.lcodes) + d.lcode_off + blk * 32;
                 for (int q = threadIdx.x; q < d.n_leaf * V; q += blockDim.x) {
                     const int l = q / V;
-                    reinterpret_cast<int4*>(scode)[q] =
-                        __ldg(reinterpret_cast<const int4*>(gcode + int64_t(l) * d.S_pad) + (q - l * V));
+                    int4 v = __ldg(reinterpret_cast<const int4*>(gcode + int64_t(l) * d.S_pad) + (q - l * V));
+                    if (!ambig) {
+                        Code* c = reinterpret_cast<Code*>(&v);
+#pragma unroll
+                        for (int e = 0; e < int(16 / sizeof(Code)); ++e)
+                            c[e] = Code(leaf_row<KP>(uint32_t(c[e]), allmask));
+                    }
+                    reinterpret_cast<int4*>(scode)[q] = v;
                 }
             }
         }
@@ -112,13 +120,12 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
         const int32_t* order = splan + H + 2;
 
         // operand of a step when it is a leaf (leaf row -op-1), as the tree-walk
-        // kernel keeps it: the selected row index or bitmask in L[0][0]'s bits, or
+        // kernel keeps it: the selected row index (or bitmask) in L[0][0]'s bits, or
         // the dense partial
         auto leaf = [&](int op, Real (&L)[1][KP]) {
             const int64_t row = int64_t(-op - 1);
             if (code_leaves) {
-                const uint32_t c = uint32_t(scode[row * 32 + lane]);
-                L[0][0] = u32_bits(ambig ? c : leaf_row<KP>(c, allmask), Real(0));
+                L[0][0] = u32_bits(uint32_t(scode[row * 32 + lane]), Real(0));
             } else {
                 ld_vec_nc<KP>(dense + (row * d.S_pad + site) * KP, L[0]);
             }
