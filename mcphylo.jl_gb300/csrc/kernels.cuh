@@ -658,6 +658,12 @@ __device__ __forceinline__ void down(const Real (&L)[SPT][KP], bool code_leaf, b
 // inside the 1e-4 per-entry gradient tolerance; FP64: IEEE division.
 __device__ __forceinline__ float ratio(float n, float d) { return __fdividef(n, d); }
 __device__ __forceinline__ double ratio(double n, double d) { return n / d; }
+// The same with a denominator shared by two ratios: FP32 keeps its reciprocal,
+// FP64 the denominator itself (IEEE division).
+__device__ __forceinline__ float den_prep(float d) { return __fdividef(1.0f, d); }
+__device__ __forceinline__ double den_prep(double d) { return d; }
+__device__ __forceinline__ float den_apply(float n, float r) { return n * r; }
+__device__ __forceinline__ double den_apply(double n, double d) { return n / d; }
 
 // Site log-likelihood of the root sum, in FP64: with lazy rescaling the root sum can
 // lie far below 1, where an FP32 logarithm would lose absolute accuracy.
@@ -872,6 +878,10 @@ prune_kernel(const PruneArgs a) {
             down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
             Real Npb[SPT][KP];
             Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
+            // wide state spaces: the gradient ratio's denominator pt_c . D_c =
+            // sum_k pb_k D0_k D1_k is the same for both children, computed once
+            constexpr bool kSharedDen = Pairs<Real, KP>::value;
+            Real den[kSharedDen ? SPT : 1];
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 // pre-order partial at the top of branch c: mother's pre times the
@@ -889,6 +899,18 @@ prune_kernel(const PruneArgs a) {
                         for (int k = 0; k < KP; ++k) pt[u][k] = pb[u][k] * D[1 - c][u][k];
                     }
                 }
+                if constexpr (kSharedDen) {
+                    if (c == 0 && (h[4] >= 0 || h[5] >= 0)) {
+#pragma unroll
+                        for (int u = 0; u < SPT; ++u) {
+                            Real s0 = Real(0), s1 = Real(0);
+#pragma unroll
+                            for (int k = 0; k < KP; k += 2)
+                                fma2(pt[u][k], pt[u][k + 1], D[0][u][k], D[0][u][k + 1], s0, s1);
+                            den[u] = den_prep(s0 + s1);
+                        }
+                    }
+                }
                 if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
                     if (c == 0) down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
@@ -896,19 +918,21 @@ prune_kernel(const PruneArgs a) {
                     Real g = Real(0);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
-                        Real num = Real(0), den = Real(0);
-                        if constexpr (Pairs<Real, KP>::value) {
+                        if constexpr (kSharedDen) {
+                            Real n0 = Real(0), n1 = Real(0);
 #pragma unroll
-                            for (int k = 0; k < KP; ++k)
-                                fma2(pt[u][k], pt[u][k], dD[u][k], D[c][u][k], num, den);
+                            for (int k = 0; k < KP; k += 2)
+                                fma2(pt[u][k], pt[u][k + 1], dD[u][k], dD[u][k + 1], n0, n1);
+                            g = fma(wtr[u], den_apply(n0 + n1, den[u]), g);
                         } else {
+                            Real num = Real(0), dn = Real(0);
 #pragma unroll
                             for (int k = 0; k < KP; ++k) {
                                 num = fma(pt[u][k], dD[u][k], num);
-                                den = fma(pt[u][k], D[c][u][k], den);
+                                dn = fma(pt[u][k], D[c][u][k], dn);
                             }
+                            g = fma(wtr[u], ratio(num, dn), g);
                         }
-                        g = fma(wtr[u], ratio(num, den), g);
                     }
                     gsum[c] = g;
                 }
