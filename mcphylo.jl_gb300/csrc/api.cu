@@ -144,11 +144,26 @@ void choose_tiles(mcphy_engine* h) {
             return;
         }
     }
+    // sites per thread: the largest the state space allows whose work items still
+    // give every SM about eight warps (more sites per thread amortise each step's
+    // record and address work; too few items leave the SMs idle)
+    const int spt_max = h->prec == MCPHY_PREC_F64 ? (h->Kp <= 4 ? 2 : 1)
+                        : h->Kp <= 4              ? 4
+                        : h->Kp == 8              ? 2
+                                                  : 1;
     int spt = h->spt_req;
-    if (spt == 0) spt = 1;
-    if (h->prec == MCPHY_PREC_F64) spt = (h->Kp <= 4) ? std::min(spt, 2) : 1;
-    else if (h->Kp == 8) spt = std::min(spt, 2);
-    else if (h->Kp > 8) spt = 1;
+    if (spt == 0) {
+        spt = 1;
+        for (int cand = spt_max; cand > 1; cand /= 2) {
+            int64_t items = 0;
+            for (const Inst& in : h->inst) items += int64_t(h->C) * ((in.S + 32 * cand - 1) / (32 * cand));
+            if (items >= int64_t(8) * h->sm_count) {
+                spt = cand;
+                break;
+            }
+        }
+    }
+    spt = std::min(spt, spt_max);
     if (spt != 1 && spt != 2 && spt != 4) spt = 1;
     h->spt = spt;
     int tpb = h->tpb_req ? h->tpb_req : 128;
