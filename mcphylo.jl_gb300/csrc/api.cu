@@ -412,10 +412,6 @@ int gather_instance(mcphy_engine* h, int64_t i) {
     g.n_blocks = d.n_blocks;
     g.slot_words = 32 * h->spt * cb / 4;
     g.row_words = int64_t(d.S_pad) * cb / 4;
-    g.code_bytes = cb;
-    g.rows = d.ambig ? 0 : 1;
-    g.kp = h->Kp;
-    g.allmask = (h->K == 32) ? 0xffffffffu : ((1u << h->K) - 1u);
     CK(launch_gather_codes(g, h->stream));
     return MCPHY_OK;
 }
@@ -455,12 +451,17 @@ int upload_data(mcphy_engine* h) {
                 }
             continue;
         }
-        // leaf-major codes, padded sites allow every state
+        // leaf-major codes, padded sites allow every state.  Without partially
+        // ambiguous codes a code is stored as the row of the step records' tables it
+        // selects: the state's index, or the row-sum row for every state (row Kp of
+        // the SIMT records, row K of the tensor-core records)
+        const uint32_t every = tc_fmt(h) >= 0 ? uint32_t(K) : uint32_t(Kp);
         for (int64_t l = 0; l < d.n_leaf; ++l) {
             const uint32_t* src = in.codes.data() + l * in.S;
             const int64_t o = h->lc_off[i] + l * d.S_pad;
             for (int64_t s = 0; s < d.S_pad; ++s) {
-                const uint32_t v = (s < in.S) ? src[s] : allmask;
+                uint32_t v = (s < in.S) ? src[s] : allmask;
+                if (!d.ambig) v = (v == allmask) ? every : uint32_t(__builtin_ctz(v));
                 if (Kp <= 8) c8[o + s] = uint8_t(v); else c32[o + s] = v;
             }
         }

@@ -108,7 +108,7 @@ struct PruneArgs {
     int32_t want_grad;
     int32_t wait_limit;       // iterations of every bounded mbarrier wait
     int32_t inject_timeout;   // test hook: never issue the first staging copy
-    const void* lcodes;       // leaf-major state codes [row][S_pad] (tensor-core path)
+    const void* lcodes;       // leaf-major state codes [row][S_pad] (level and tensor-core paths)
     const SchedNode* sched;   // schedule nodes (tensor-core path: sweep prologues)
     const double* weights;    // site-pattern weights per instance [S_pad], 0 past S
     const int32_t* plan;      // level plans (level-synchronous sweep), per instance at plan_off
@@ -596,11 +596,6 @@ __device__ __forceinline__ double u32_bits(uint32_t c, double) { return __longlo
 __device__ __forceinline__ uint32_t bits_u32(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ uint32_t bits_u32(double v) { return uint32_t(__double_as_longlong(v)); }
 
-template <int KP>
-__device__ __forceinline__ uint32_t leaf_row(uint32_t code, uint32_t allmask) {
-    return code == allmask ? uint32_t(KP) : uint32_t(__ffs(int(code)) - 1);
-}
-
 // Sum of the rows of T selected by a state bitmask (a partially ambiguous leaf).
 template <int KP, typename Real>
 __device__ __forceinline__ void leaf_down_mask(const Real* T, uint32_t code, Real (&D)[KP]) {
@@ -628,9 +623,9 @@ __device__ __forceinline__ void write_vec(Real* v, int lane, const Real (&L)[SPT
 #pragma unroll
     for (int u = 0; u < SPT; ++u) st_vec<KP>(v + (u * 32 + lane) * KP, L[u]);
 }
-// Leaf codes of the warp's sites in a ring slot.  The schedule-ordered copy holds
-// row indices already (0..K-1 one state, KP every state) for instances without
-// partially ambiguous codes, else the raw bitmasks (gather_codes_kernel).
+// Leaf codes of the warp's sites in a ring slot: table rows (0..K-1 one state, KP
+// every state) for instances without partially ambiguous codes, else the raw
+// bitmasks (decoded at upload).
 template <int KP, int SPT, typename Real>
 __device__ __forceinline__ void read_codes(const unsigned char* p, int lane, Real (&L)[SPT][KP]) {
     using Code = typename CodeOf<KP>::type;
@@ -1116,11 +1111,6 @@ struct GatherArgs {
     int32_t n_blocks;
     int32_t slot_words;       // site block x code bytes / 4
     int64_t row_words;        // S_pad x code bytes / 4
-    int32_t code_bytes;       // 1 (K <= 8) or 4
-    int32_t rows;             // 1: store row indices (the instance has no partially
-                              // ambiguous codes): one state s -> s, every state -> Kp
-    int32_t kp;
-    uint32_t allmask;
 };
 cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st);
 

@@ -110,22 +110,7 @@ __global__ void __launch_bounds__(256) gather_codes_kernel(const GatherArgs a) {
         const int32_t op = a.sched[j].op[c];
         if (op >= 0) continue;
         const int64_t row = -int64_t(op) - 1;
-        uint32_t v = __ldg(a.src + row * a.row_words + b * a.slot_words + w);
-        if (a.rows) {
-            // one state: its index; every state: Kp (the row-sum row of a record)
-            auto to_row = [&](uint32_t c) -> uint32_t {
-                return c == a.allmask ? uint32_t(a.kp) : uint32_t(__ffs(int(c)) - 1);
-            };
-            if (a.code_bytes == 1) {
-                uint32_t r = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) r |= to_row((v >> (8 * q)) & 0xffu) << (8 * q);
-                v = r;
-            } else {
-                v = to_row(v);
-            }
-        }
-        a.dst[idx] = v;
+        a.dst[idx] = __ldg(a.src + row * a.row_words + b * a.slot_words + w);
     }
 }
 

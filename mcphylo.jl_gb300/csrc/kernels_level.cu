@@ -68,7 +68,6 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
     Real* sroot = reinterpret_cast<Real*>(smem + lay.root);
     int32_t* splan = reinterpret_cast<int32_t*>(smem + lay.plan);
     Code* scode = reinterpret_cast<Code*>(smem + lay.code);
-    const uint32_t allmask = (a.K >= 32) ? 0xffffffffu : ((1u << a.K) - 1u);
     const int C = a.C;
 
     for (int t = blockIdx.x; t < a.n_items; t += gridDim.x) {
@@ -96,21 +95,14 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
             const int32_t* gplan = a.plan + d.plan_off;
             for (int q = threadIdx.x; q < 2 * J + 2; q += blockDim.x) splan[q] = __ldg(gplan + q);
             if (code_leaves) {
-                // row l: sites blk*32 .. +32 of the leaf-major copy, 32 * sizeof(Code) bytes,
-                // stored as the row of the record's tables each code selects (the state's
-                // index, KP for every state) unless the instance has partially ambiguous codes
+                // row l: sites blk*32 .. +32 of the leaf-major copy, 32 * sizeof(Code)
+                // bytes (table rows, or bitmasks for partially ambiguous instances)
                 constexpr int V = 32 * int(sizeof(Code)) / 16;   // int4 per row
                 const Code* gcode = reinterpret_cast<const Code*>(a.lcodes) + d.lcode_off + blk * 32;
                 for (int q = threadIdx.x; q < d.n_leaf * V; q += blockDim.x) {
                     const int l = q / V;
-                    int4 v = __ldg(reinterpret_cast<const int4*>(gcode + int64_t(l) * d.S_pad) + (q - l * V));
-                    if (!ambig) {
-                        Code* c = reinterpret_cast<Code*>(&v);
-#pragma unroll
-                        for (int e = 0; e < int(16 / sizeof(Code)); ++e)
-                            c[e] = Code(leaf_row<KP>(uint32_t(c[e]), allmask));
-                    }
-                    reinterpret_cast<int4*>(scode)[q] = v;
+                    reinterpret_cast<int4*>(scode)[q] =
+                        __ldg(reinterpret_cast<const int4*>(gcode + int64_t(l) * d.S_pad) + (q - l * V));
                 }
             }
         }

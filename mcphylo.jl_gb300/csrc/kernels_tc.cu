@@ -173,10 +173,27 @@ __device__ __forceinline__ void zero(float (&v)[KD]) {
 }
 
 // Down vector of a leaf from a record table (K rows of K4, zero beyond K) and its
-// row sums (K4 entries, zero beyond K); 16-byte loads.
+// row sums (K4 entries, zero beyond K, stored right after the table); 16-byte loads.
+// rows: the code is the table row itself (a state's index, K for every state: the
+// row sums), as uploaded for instances without partially ambiguous codes; else a
+// state bitmask.
 template <int KD>
-__device__ __forceinline__ void leaf_down(uint32_t code, uint32_t allmask, const float* tab,
-                                          const float* rs, int K, int K4, float (&out)[KD]) {
+__device__ __forceinline__ void leaf_down(uint32_t code, bool rows, uint32_t allmask,
+                                          const float* tab, const float* rs, int K, int K4,
+                                          float (&out)[KD]) {
+    if (rows) {
+        const float* row = tab + code * K4;
+#pragma unroll
+        for (int k = 0; k < KD; k += 4) {
+            if (k < K4) {
+                const float4 x = *reinterpret_cast<const float4*>(row + k);
+                out[k] = x.x; out[k + 1] = x.y; out[k + 2] = x.z; out[k + 3] = x.w;
+            } else {
+                out[k] = 0.f; out[k + 1] = 0.f; out[k + 2] = 0.f; out[k + 3] = 0.f;
+            }
+        }
+        return;
+    }
     zero(out);
     const float* row = nullptr;
     if (code == allmask) row = rs;
@@ -391,6 +408,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         const int item = __ldg(a.queue + qi);
         const int2 it = __ldg(a.items + item);
         const InstanceDesc d = a.inst[it.x];
+        const bool rows = d.ambig == 0;   // leaf codes are table rows
         const int r = it.y / d.n_blocks;
         const int blk = it.y - r * d.n_blocks;
         const int site = blk * TC_M + t;
@@ -445,10 +463,10 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 }
             }
             if (op0 < 0)
-                leaf_down<VK>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K, FMT)),
+                leaf_down<VK>(code0, rows, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K, FMT)),
                               reinterpret_cast<const float*>(f0 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D0);
             if (op1 < 0)
-                leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
+                leaf_down<VK>(code1, rows, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
                               reinterpret_cast<const float*>(f1 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D1);
             mul_v<VK>(D0, D1, D0);
             eacc += rescale<VK, float>(D0);
@@ -560,13 +578,13 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             if (op0 >= 0) {
                 if (okr) tmem_row<VK>(tl + 0, D0);
             } else {
-                leaf_down<VK>(code0, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K, FMT)),
+                leaf_down<VK>(code0, rows, allmask, reinterpret_cast<const float*>(f0 + tc_tile(K, FMT)),
                               reinterpret_cast<const float*>(f0 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D0);
             }
             if (op1 >= 0) {
                 if (okr) tmem_row<VK>(tl + 64, D1);
             } else {
-                leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
+                leaf_down<VK>(code1, rows, allmask, reinterpret_cast<const float*>(f1 + tc_tile(K, FMT)),
                               reinterpret_cast<const float*>(f1 + tc_tile(K, FMT) + tc_tab(K)), K, K4, D1);
             }
             // child 1: pt_1 = pb * D_0; child 0: pt_0 = pb * D_1
@@ -576,7 +594,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 if (op1 >= 0) {
                     if (okr) tmem_row<VK>(tl + 96, dD);
                 } else {
-                    leaf_down<VK>(code1, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K, FMT)),
+                    leaf_down<VK>(code1, rows, allmask, reinterpret_cast<const float*>(k1 + 2 * tc_tile(K, FMT)),
                                   reinterpret_cast<const float*>(k1 + 2 * tc_tile(K, FMT) + tc_tab(K)), K,
                                   K4, dD);
                 }
@@ -591,7 +609,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 if (op0 >= 0) {
                     if (okr) tmem_row<VK>(tl + 32, dD);
                 } else {
-                    leaf_down<VK>(code0, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K, FMT)),
+                    leaf_down<VK>(code0, rows, allmask, reinterpret_cast<const float*>(k0 + 2 * tc_tile(K, FMT)),
                                   reinterpret_cast<const float*>(k0 + 2 * tc_tile(K, FMT) + tc_tab(K)), K,
                                   K4, dD);
                 }
