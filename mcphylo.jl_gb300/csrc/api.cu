@@ -145,8 +145,9 @@ void choose_tiles(mcphy_engine* h) {
         }
     }
     // sites per thread: the largest the state space allows whose work items still
-    // give every SM about eight warps (more sites per thread amortise each step's
-    // record and address work; too few items leave the SMs idle)
+    // give every SM about sixteen warps, two rounds of the resident warps (more sites
+    // per thread amortise each step's record and address work; with fewer items the
+    // last round runs partly empty)
     const int spt_max = h->prec == MCPHY_PREC_F64 ? (h->Kp <= 4 ? 2 : 1)
                         : h->Kp <= 4              ? 4
                         : h->Kp == 8              ? 2
@@ -157,7 +158,7 @@ void choose_tiles(mcphy_engine* h) {
         for (int cand = spt_max; cand > 1; cand /= 2) {
             int64_t items = 0;
             for (const Inst& in : h->inst) items += int64_t(h->C) * ((in.S + 32 * cand - 1) / (32 * cand));
-            if (items >= int64_t(8) * h->sm_count) {
+            if (items >= int64_t(16) * h->sm_count) {
                 spt = cand;
                 break;
             }

@@ -265,11 +265,21 @@ def engine_posterior(parent, blen, codes, leaf_nums, model_out, pi, rates, prior
 
     U, D, Uinv, mu = model_out
     engines = []
+    tiles = sweep = None
     for _ in range(2 if proposals else 1):
         e = Engine(len(pi), len(rates), precision)
         e.set_tree(parent, blen)
         e.set_codes(codes, leaf_nums)
         e.set_model(U, D, Uinv, mu, pi, rates)
+        if tiles is None:
+            # a chain evaluates the same problem thousands of times: time the launch
+            # shapes once, and give the proposal engine the same one
+            tiles = e.autotune()
+            sweep = e.sweep() if precision in ("f32", "f64") else None
+        else:
+            e.set_tiles(*tiles)
+            if sweep is not None:
+                e.set_sweep(sweep)
         if graph:
             e.enable_graph(True)
         engines.append(e)
