@@ -347,7 +347,10 @@ def run_nuts(args):
         raise SystemExit("--mode nuts runs on a single-tree workload")
     inst = insts[0]
     prior = P.CompoundDirichlet(*NUTS_PRIOR)
-    n_iter, n_adapt = args.nuts_iter, args.nuts_adapt
+    # the benchmark's chain lengths: 1000 iterations on the 32-taxon restriction
+    # workload, 2000 on the 512-taxon birth-death one
+    n_iter = args.nuts_iter or (2000 if args.workload == "restriction-g4-bd" else 1000)
+    n_adapt = args.nuts_adapt
     res = {}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         for prec in ("f32", "f64"):
@@ -708,7 +711,8 @@ def main():
     ap.add_argument("--mode", default="grad", choices=["grad", "logl", "nuts"],
                     help="grad: logL + gradient (the headline metric); logl: logL only; "
                          "nuts: PNUTS ESS/s on a single-tree workload")
-    ap.add_argument("--nuts-iter", type=int, default=1000)
+    ap.add_argument("--nuts-iter", type=int, default=0,
+                    help="sampling iterations (0: 2000 on restriction-g4-bd, else 1000)")
     ap.add_argument("--nuts-adapt", type=int, default=200)
     ap.add_argument("--nuts-seed", type=int, default=1)
     ap.add_argument("--nuts-target", type=float, default=0.8)
