@@ -182,20 +182,32 @@ class CompoundDirichlet:
     beta: float = 0.1
     c: float = 1.0
 
+    def _topology(self, parent):
+        """Per topology (cached): the weight of each log branch length, a - 1 for a
+        leaf branch and a c - 1 for an internal one, and the exponent of the tree
+        length, alpha - a n_term - a c (n_term - 3)."""
+        cache = self.__dict__.setdefault("_cache", {})
+        key = np.ascontiguousarray(parent, dtype=np.int64).tobytes()
+        hit = cache.get(key)
+        if hit is None:
+            internal = internal_external(parent) == 1
+            a, c = self.a, self.c
+            nterm = float(np.sum(~internal))
+            w = np.where(internal, a * c - 1.0, a - 1.0)
+            coef = self.alpha - a * nterm - a * c * (nterm - 3.0)
+            if len(cache) >= 64:
+                cache.clear()
+            hit = cache[key] = (w, coef)
+        return hit
+
     def logpdf_grad(self, parent, blen):
         blen = np.asarray(blen, dtype=np.float64)
-        internal = internal_external(parent) == 1
-        t_l = float(np.sum(blen))
-        nterm = float(np.sum(~internal))
-        n_int = nterm - 3.0
+        w, coef = self._topology(parent)
         al, a, be, c = self.alpha, self.a, self.beta, self.c
-        coef = al - a * nterm - a * c * n_int
-        v = (al * math.log(be) - gammaln(al) - t_l * be
-             - gammaln(a) - gammaln(c) + gammaln(a + c)
-             + float(np.sum(np.log(blen[~internal]))) * (a - 1.0)
-             + float(np.sum(np.log(blen[internal]))) * (a * c - 1.0)
-             + coef * math.log(t_l))
-        g = np.where(internal, (a * c - 1.0) / blen, (a - 1.0) / blen) - be + coef / t_l
+        t_l = float(np.sum(blen))
+        const = al * math.log(be) - gammaln(al) - gammaln(a) - gammaln(c) + gammaln(a + c)
+        v = const - t_l * be + float(np.dot(w, np.log(blen))) + coef * math.log(t_l)
+        g = w / blen + (coef / t_l - be)
         return float(v), g
 
 
