@@ -7,9 +7,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <new>
 #include <numeric>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -1221,15 +1223,20 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
         int sweep, spt, tpb;
     };
     std::vector<Cand> cand;
-    if (h->prec == MCPHY_PREC_F64)
-        cand = h->Kp <= 4 ? std::vector<Cand>{{1, 1, 128}, {1, 2, 128}, {1, 1, 64}, {1, 2, 64}}
-                          : std::vector<Cand>{{1, 1, 128}, {1, 1, 64}};
-    else if (h->Kp <= 4)
-        cand = {{1, 4, 128}, {1, 4, 64}, {1, 2, 128}, {1, 2, 64}, {1, 4, 256}, {1, 1, 128}};
-    else if (h->Kp <= 8)
-        cand = {{1, 1, 128}, {1, 2, 128}, {1, 1, 64}, {1, 2, 64}};
-    else
-        cand = {{1, 1, 64}, {1, 1, 128}, {1, 1, 32}};
+    // tree-walk shapes (sites per thread, threads per block)
+    auto walk = [&](std::initializer_list<std::pair<int, int>> shapes) {
+        for (const auto& st : shapes) cand.push_back({MCPHY_SWEEP_WALK, st.first, st.second});
+    };
+    if (h->prec == MCPHY_PREC_F64) {
+        if (h->Kp <= 4) walk({{1, 128}, {2, 128}, {1, 64}, {2, 64}});
+        else walk({{1, 128}, {1, 64}});
+    } else if (h->Kp <= 4) {
+        walk({{4, 128}, {4, 64}, {2, 128}, {2, 64}, {4, 256}, {1, 128}});
+    } else if (h->Kp <= 8) {
+        walk({{1, 128}, {2, 128}, {1, 64}, {2, 64}});
+    } else {
+        walk({{1, 64}, {1, 128}, {1, 32}});
+    }
     // the level sweep where an item fits a CTA and the walk cannot fill the GPU
     if (h->dirty & DIRTY_LAYOUT) {
         int rc0 = prepare(h);
