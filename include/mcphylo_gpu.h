@@ -150,16 +150,20 @@ int mcphy_logpdf_device(mcphy_handle h, double* d_ll);
  * No counterpart in the reference: an extension for callers that cannot allocate
  * device memory while they evaluate (cudaMalloc synchronises the whole device and
  * may be forbidden inside their loop or outside their own memory budget).  Same
- * result as mcphy_batch_logpdf_grad for the branch lengths in d_blen_packed (device
- * memory, packed by instance), written to d_ll[M] and d_grad_packed (device
- * memory), asynchronously on the handle's stream.  It allocates nothing: its
- * scratch is one fixed 64 MiB device array inside the library, shared by every
- * call in the process (calls whose GPU work overlaps race; serialise them); only
- * the work counter in it is cleared per call.  Problems whose per-item partial
- * sums exceed the array are rejected with MCPHY_ERR_ARG.  Tree, data and model
- * must have been uploaded by a regular evaluation since they last changed
- * (MCPHY_ERR_STATE otherwise).  The first call on a device looks up the array's
- * device address; make it before any stream capture. */
+ * result as mcphy_batch_logpdf_grad, bit for bit, for the branch lengths in
+ * d_blen_packed (device memory, packed by instance), written to d_ll[M] and
+ * d_grad_packed (device memory), asynchronously on the handle's stream.  It
+ * allocates nothing: its scratch is one fixed 64 MiB device array inside the
+ * library, shared by every call in the process (calls whose GPU work overlaps race;
+ * serialise them); only the work counter and error flag in it are cleared per call.
+ * Problems whose per-item partial sums exceed the array are rejected with
+ * MCPHY_ERR_ARG.  Tree, data and model must have been uploaded by a regular
+ * evaluation since they last changed (MCPHY_ERR_STATE otherwise).  Branch lengths
+ * are not validated here: pass finite, non-negative values.  A bounded device wait
+ * that gives up cannot be reported in the status (the call returns before the GPU
+ * work ends): every output entry is written as NaN instead.  The first call on a
+ * device (per device context) looks up the array's device address; make it before
+ * any stream capture. */
 int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_packed, double* d_ll,
                               double* d_grad_packed);
 
@@ -226,6 +230,12 @@ const char* mcphy_last_error(mcphy_handle h);
  * allocation fail (MCPHY_ERR_OOM); the handle keeps its state and the next call
  * retries.  kind 0 clears either. */
 int mcphy_debug_inject(mcphy_handle h, int kind);
+/* Self-check of the per-device record of the dynamic shared memory each kernel is
+ * allowed (a kernel attribute is set on the current device only, so a process that
+ * drives several GPUs raises it once per device), run against a fake attribute
+ * setter from several host threads.  Needs no device.  Returns 0, or the number of
+ * the check that failed.  No counterpart in the reference. */
+int mcphy_debug_check_allowance(void);
 const char* mcphy_status_string(int status);
 /* Library version as major*10000 + minor*100 + patch. */
 int mcphy_version(void);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -11,6 +12,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -18,6 +20,7 @@
 
 #include "engine_state.h"
 #include "kernels.cuh"
+#include "launch_attr.h"
 #include "mcphy_internal.h"
 #include "mcphylo_gpu.h"
 
@@ -1198,6 +1201,71 @@ int mcphy_debug_inject(mcphy_handle h, int kind) {
     if (kind < 0 || kind > 2) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
     h->inject = kind;
     return MCPHY_OK;
+}
+
+int mcphy_debug_check_allowance(void) {
+    // 1: the first raise on a device sets the attribute once
+    {
+        SmemAllowance a;
+        int calls = 0;
+        auto set = [&](int) { ++calls; return cudaSuccess; };
+        if (a.raise(0, 1000, set) != cudaSuccess || calls != 1 || a.allowed(0) != 1000) return 1;
+        // 2: a smaller or equal size on the same device sets nothing
+        if (a.raise(0, 500, set) != cudaSuccess || a.raise(0, 1000, set) != cudaSuccess || calls != 1)
+            return 2;
+        // 3: another device has its own record
+        if (a.raise(1, 500, set) != cudaSuccess || calls != 2 || a.allowed(1) != 500 ||
+            a.allowed(0) != 1000)
+            return 3;
+        // 4: a failed set leaves the record as it was, and the next raise retries
+        auto bad = [&](int) { ++calls; return cudaErrorInvalidValue; };
+        if (a.raise(1, 800, bad) != cudaErrorInvalidValue || a.allowed(1) != 500) return 4;
+        if (a.raise(1, 800, set) != cudaSuccess || a.allowed(1) != 800) return 4;
+        // 5: device ordinals outside the record are refused without a set
+        const int before = calls;
+        if (a.raise(-1, 10, set) != cudaErrorInvalidDevice ||
+            a.raise(kMaxDevices, 10, set) != cudaErrorInvalidDevice || calls != before)
+            return 5;
+    }
+    // 6: raises from several threads on several devices: every device ends at the
+    // largest size asked for, the setter ran only for increases (never lowering), and
+    // no two setters of one device overlapped
+    {
+        SmemAllowance a;
+        constexpr int kDev = 4, kThreads = 8, kIters = 2000;
+        std::atomic<int> inside[kDev];
+        std::atomic<int> last[kDev];
+        std::atomic<int> bad{0};
+        for (int d = 0; d < kDev; ++d) {
+            inside[d] = 0;
+            last[d] = 0;
+        }
+        std::vector<std::thread> th;
+        for (int t = 0; t < kThreads; ++t)
+            th.emplace_back([&, t]() {
+                for (int i = 0; i < kIters; ++i) {
+                    const int d = (i + t) % kDev;
+                    const int bytes = 1 + (i * 7919 + t * 104729) % 50000;
+                    a.raise(d, bytes, [&](int b) {
+                        if (inside[d].fetch_add(1) != 0) bad = 1;
+                        if (b <= last[d].load()) bad = 1;
+                        last[d] = b;
+                        inside[d].fetch_sub(1);
+                        return cudaSuccess;
+                    });
+                }
+            });
+        for (auto& x : th) x.join();
+        if (bad) return 6;
+        for (int d = 0; d < kDev; ++d) {
+            int want = 0;
+            for (int t = 0; t < kThreads; ++t)
+                for (int i = 0; i < kIters; ++i)
+                    if ((i + t) % kDev == d) want = std::max(want, 1 + (i * 7919 + t * 104729) % 50000);
+            if (a.allowed(d) != want || last[d] != want) return 6;
+        }
+    }
+    return 0;
 }
 
 int mcphy_enable_graph(mcphy_handle h, int on) {

@@ -25,6 +25,7 @@
 #include <algorithm>
 
 #include "kernels.cuh"
+#include "launch_attr.h"
 
 namespace mcphy {
 
@@ -225,18 +226,15 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
     }
 }
 
-// Dynamic shared memory allowed for each instantiation: raised to the largest size
-// any layout asked for and never lowered (handles of different sizes share it).
-// Raised by the layout's occupancy query and by the first, eager evaluation of a
-// layout, never inside a stream capture.
+// Dynamic shared memory allowed for each instantiation, per device: raised to the
+// largest size any layout asked for and never lowered (launch_attr.h).
 template <int KP, typename Real>
 static cudaError_t allow_smem(int smem) {
-    static int allowed = 0;
-    if (smem <= allowed) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(prune_level_kernel<KP, Real>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) allowed = smem;
-    return e;
+    static SmemAllowance allowance;
+    return raise_smem(allowance, smem, [](int bytes) {
+        return cudaFuncSetAttribute(prune_level_kernel<KP, Real>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    });
 }
 
 template <int KP, typename Real>

@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include "kernels.cuh"
+#include "launch_attr.h"
 #include "tc.cuh"
 
 namespace mcphy {
@@ -694,19 +695,25 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
     if (warp == 0) tc::tmem_dealloc(tbase, kTmemCols);
 }
 
+// Shared-memory allowance and carveout of each instantiation, per device
+// (launch_attr.h).
+template <int VK, int FMT>
+cudaError_t allow_tc(int smem) {
+    static SmemAllowance allowance;
+    return raise_smem(allowance, smem, [](int bytes) {
+        cudaError_t e = cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>,
+                                    cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    });
+}
+
 template <int VK, int FMT>
 cudaError_t go_tc(int blocks, const PruneArgs& a, cudaStream_t st) {
     const int smem = tc_smem_bytes(a.K, FMT);
-    static int configured = 0;
-    if (smem > configured) {
-        cudaError_t e =
-            cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 100);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    cudaError_t e = allow_tc<VK, FMT>(smem);
+    if (e != cudaSuccess) return e;
     prune_tc_kernel<VK, FMT><<<blocks, TC_M, smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -714,10 +721,7 @@ cudaError_t go_tc(int blocks, const PruneArgs& a, cudaStream_t st) {
 template <int VK, int FMT>
 cudaError_t occ_tc(int K, int* bps) {
     const int smem = tc_smem_bytes(K, FMT);
-    cudaError_t e =
-        cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(prune_tc_kernel<VK, FMT>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaError_t e = allow_tc<VK, FMT>(smem);
     if (e != cudaSuccess) return e;
     // resident CTAs per SM from the kernel's own limits: registers (allocated per
     // warp in units of 256), shared memory (plus the 1 KB each CTA reserves) and

@@ -16,23 +16,37 @@
 //   - a problem whose per-item partial sums do not fit is rejected with
 //     MCPHY_ERR_ARG and a message giving the bytes it would need; the number
 //     of resident blocks of the fused kernel is reduced until the per-warp
-//     partials fit (fewer blocks: slower, same results);
+//     partials fit (fewer blocks: slower, same results, bit for bit);
 //   - every call, from every handle in the process, uses the same array and
 //     leaves its contents behind (only the work counter and the error flag are
-//     cleared per call; a staging timeout is not reported by this entry point),
-//     so calls whose GPU work overlaps (different streams, different host
-//     threads) race and must be serialised by the caller;
-//   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture begins.
+//     cleared per call), so calls whose GPU work overlaps (different streams,
+//     different host threads) race and must be serialised by the caller;
+//   - the call returns before the GPU work ends, so a bounded wait that gives up
+//     in the sweep cannot be reported in the status: the results are written as
+//     NaN instead (the log-likelihood of every instance and every gradient entry),
+//     which a caller following the reference's rule (a NaN gradient becomes -Inf,
+//     a rejected proposal) treats as a failed evaluation;
+//   - branch lengths are read straight from the caller's device array and are not
+//     validated: they must be finite and non-negative (the regular entry points
+//     reject others with MCPHY_ERR_DATA; here they give NaN or meaningless
+//     results);
+//   - the first call on a device (more precisely, in a device context) looks up
+//     the array's device address with cudaGetSymbolAddress, with that device
+//     current; make that first call before any stream capture begins.  A
+//     cudaDeviceReset ends the context: the address is looked up again in the
+//     new one (every handle made before the reset is unusable anyway).
+#include <cuda.h>   // CUcontext / CUresult types only: the driver call goes through
+                    // the runtime's entry-point lookup, no link against libcuda
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <mutex>
 #include <string>
 
 #include "engine_state.h"
 #include "kernels.cuh"
+#include "launch_attr.h"
 #include "mcphylo_gpu.h"
 
 using namespace mcphy;
@@ -40,18 +54,40 @@ using namespace mcphy;
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;   // 64 MiB
-constexpr int kMaxDevices = 64;
 
 // The scratch every allocation-free call shares (device memory, fixed size).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
+// cuCtxGetCurrent through the runtime's driver entry-point lookup (null if absent)
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+CtxGetCurrent ctx_get_current() {
+    static const CtxGetCurrent fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return CtxGetCurrent(nullptr);
+        }
+        return reinterpret_cast<CtxGetCurrent>(p);
+    }();
+    return fn;
+}
+
 std::mutex g_addr_mu;
-void* g_addr[kMaxDevices] = {nullptr};
+struct ScratchAddr {
+    CUcontext ctx = nullptr;   // context the address was looked up in
+    void* addr = nullptr;
+};
+ScratchAddr g_addr[kMaxDevices];
 
 size_t round_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Device address of g_noalloc_scratch on the current device, looked up once per
-// device.  In host code the symbol is only a host-side stand-in.
+// device context.  In host code the symbol is only a host-side stand-in: a kernel
+// given it would fault or, where the GPU can reach host memory, use the wrong
+// memory.
 int scratch_address(mcphy_engine* h, void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -63,8 +99,11 @@ int scratch_address(mcphy_engine* h, void** out) {
         h->err = "device ordinal out of range for the allocation-free scratch";
         return MCPHY_ERR_ARG;
     }
+    CUcontext ctx = nullptr;
+    if (CtxGetCurrent f = ctx_get_current()) f(&ctx);
     std::lock_guard<std::mutex> lock(g_addr_mu);
-    if (!g_addr[dev]) {
+    ScratchAddr& a = g_addr[dev];
+    if (!a.addr || a.ctx != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr) {
@@ -72,10 +111,23 @@ int scratch_address(mcphy_engine* h, void** out) {
                      cudaGetErrorString(e);
             return MCPHY_ERR_CUDA;
         }
-        g_addr[dev] = p;
+        a.addr = p;
+        a.ctx = ctx;
     }
-    *out = g_addr[dev];
+    *out = a.addr;
     return MCPHY_OK;
+}
+
+// Copies the reduced results [ll (M) | gradient (total_branch)] to the caller's
+// arrays; when the sweep's error flag is set (a bounded wait gave up), every
+// output entry becomes NaN instead.
+__global__ void noalloc_finish_kernel(const double* out, const int32_t* flag, double* ll,
+                                      double* grad, int64_t M, int64_t total_branch) {
+    const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= M + total_branch) return;
+    const double v = (*flag != 0) ? __longlong_as_double(0x7ff8000000000000ll) : out[e];
+    if (e < M) ll[e] = v;
+    else grad[e - M] = v;
 }
 
 #define NA_CK(call)                                                                    \
@@ -196,9 +248,12 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     a.K = h->K;
     a.C = h->C;
     a.want_grad = 1;
-    a.wait_limit = kWaitLimit;
+    // test hook (mcphy_debug_inject kind 1): the first staging copy is never issued,
+    // so its bounded wait runs out
+    a.wait_limit = h->inject == 1 ? 4096 : kWaitLimit;
+    a.inject_timeout = h->inject == 1 ? 1 : 0;
+    if (h->inject == 1) h->inject = 0;
     a.weights = static_cast<const double*>(h->d_weights.p);
-    a.inject_timeout = 0;
     a.lcodes = h->d_leafcodes.p;
     a.plan = static_cast<const int32_t*>(h->d_plan.p);
     a.max_J = h->max_J;
@@ -218,9 +273,9 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     r.part = reinterpret_cast<double*>(s + off_part);
     r.out = reinterpret_cast<double*>(s + off_out);
     NA_CK(launch_reduce(f64, r, h->max_branch, st));
-    NA_CK(cudaMemcpyAsync(d_ll, s + off_out, sizeof(double) * size_t(h->M),
-                          cudaMemcpyDeviceToDevice, st));
-    NA_CK(cudaMemcpyAsync(d_grad_packed, s + off_out + sizeof(double) * size_t(h->M),
-                          sizeof(double) * size_t(h->total_branch), cudaMemcpyDeviceToDevice, st));
+    const int64_t n_res = h->M + h->total_branch;
+    noalloc_finish_kernel<<<unsigned((n_res + 255) / 256), 256, 0, st>>>(
+        r.out, a.counter + 1, d_ll, d_grad_packed, h->M, h->total_branch);
+    NA_CK(cudaGetLastError());
     return MCPHY_OK;
 }

@@ -67,6 +67,7 @@ SIGNATURES = {
     "mcphy_get_sweep": (c_int, [handle_t, P(c_int)]),
     "mcphy_enable_graph": (c_int, [handle_t, c_int]),
     "mcphy_debug_inject": (c_int, [handle_t, c_int]),
+    "mcphy_debug_check_allowance": (c_int, []),
     "mcphy_enable_timing": (c_int, [handle_t, c_int]),
     "mcphy_get_timing": (c_int, [handle_t, P(ctypes.c_float)]),
     "mcphy_get_counts": (c_int, [handle_t, pi64]),

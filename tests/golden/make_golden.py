@@ -1,7 +1,11 @@
 """Generate the golden fixtures under tests/golden/ from the reference's own tests.
 
-Run in a container where the reference project is mounted (default path below,
-override with MCPHYLO_REFERENCE).  It reads the reference's test files as text:
+Run where the reference project is checked out, giving its root directory as the
+first argument or in MCPHYLO_REFERENCE:
+
+    python tests/golden/make_golden.py <path to MCPhylo.jl>
+
+It reads the reference's test files as text:
 
 * test/likelihood/felsenstein.jl:2-41   -> Newick strings, logL and gradient goldens
 * test/likelihood/{primates,simudata}.nex -> the alignments (stored as taxon names +
@@ -18,7 +22,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("MCPHYLO_REFERENCE", "/root/reference")
+REF = None   # the reference's root directory, set by main()
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -111,4 +115,7 @@ def main():
 
 
 if __name__ == "__main__":
+    REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MCPHYLO_REFERENCE")
+    if not REF or not os.path.isdir(os.path.join(REF, "test", "likelihood")):
+        sys.exit("usage: make_golden.py <MCPhylo.jl root> (or set MCPHYLO_REFERENCE)")
     main()

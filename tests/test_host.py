@@ -31,6 +31,14 @@ def test_library_exports_every_declared_symbol(built_lib):
     assert sorted(_lib.SIGNATURES) == names
 
 
+def test_smem_allowance_is_per_device_and_thread_safe(built_lib):
+    """The record of each kernel's dynamic shared-memory allowance is kept per
+    device and behind a mutex (a kernel attribute is set on the current device
+    only), checked against a fake setter from several threads: no GPU needed."""
+    L = _lib.load()
+    assert L.mcphy_debug_check_allowance() == 0
+
+
 def test_version_and_status_strings(built_lib):
     L = _lib.load()
     assert L.mcphy_version() >= 100
