@@ -597,15 +597,21 @@ def run_gpu(args, rank, world):
         ll64 = np.atleast_1d(ll64)
         rel_tot = abs(ll32_last.sum() - ll64.sum()) / abs(ll64.sum())
         rel_inst = np.max(np.abs(ll32_last - ll64) / np.abs(ll64))
-        rel_g = None
+        rel_g = rel_g_raw = within = None
         if g64 is not None:
             gscale = np.zeros_like(g64)
             for i in range(M):
                 s = slice(off[i], off[i + 1])
                 gscale[s] = np.maximum(np.abs(g64[s]), 1e-2 * np.abs(g64[s]).max())
             rel_g = float(np.max(np.abs(g32_last - g64) / gscale))
+            # per entry without a floor: |g32_i - g64_i| / |g64_i|
+            raw = np.abs(g32_last - g64) / np.maximum(np.abs(g64), 1e-300)
+            rel_g_raw = float(np.max(raw))
+            within = float(np.mean(raw <= 1e-4))
         err = {"logl_total_rel": float(rel_tot), "logl_max_instance_rel": float(rel_inst),
                "grad_max_entry_rel": rel_g, "grad_floor": "1e-2 x max |g| of the instance",
+               "grad_max_entry_rel_unfloored": rel_g_raw,
+               "grad_entries_within_1e-4_unfloored": within,
                "within_1e-6": bool(rel_inst <= 1e-6)}
         e64.close()
 

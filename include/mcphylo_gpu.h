@@ -228,7 +228,10 @@ const char* mcphy_last_error(mcphy_handle h);
  * MCPHY_ERR_TIMEOUT and later ones are unaffected (tree-walk and tensor-core sweeps;
  * the level sweep stages nothing and has no waits).  kind 2 makes the next device
  * allocation fail (MCPHY_ERR_OOM); the handle keeps its state and the next call
- * retries.  kind 0 clears either. */
+ * retries.  kind 3 makes the tree walk run its general kernel (the one for dense
+ * leaves and partially ambiguous codes) on every instance, for comparing it with the
+ * row-code kernel the handle would otherwise use; it stays until kind 0 is set.
+ * kind 0 clears all of them. */
 int mcphy_debug_inject(mcphy_handle h, int kind);
 /* Self-check of the per-device record of the dynamic shared memory each kernel is
  * allowed (a kernel attribute is set on the current device only, so a process that

@@ -22,7 +22,7 @@ LIB = os.path.join(HERE, "mcphylo_gb300", "libmcphylo_gpu.so")
 SOURCES = ["schedule.cpp", "api.cu", "noalloc.cu", "kernels_common.cu", "kernels_f32.cu",
            "kernels_f64.cu", "kernels_tc.cu", "kernels_level.cu", "tc_selftest.cu"]
 HEADERS = ["mcphy_internal.h", "kernels.cuh", "engine_state.h", "tc.cuh", "launch_attr.h",
-           "prune_launch.cuh"]
+           "prune_launch.cuh", "kernels_walk.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -45,6 +45,16 @@ int kp_of(int K) {
     return 0;
 }
 
+// Whether some code allows more than one state but not all of them (or none).
+bool any_ambiguous(const uint32_t* codes, int64_t n, int K) {
+    const uint32_t allmask = (K == 32) ? 0xffffffffu : ((1u << K) - 1u);
+    for (int64_t e = 0; e < n; ++e) {
+        const uint32_t c = codes[e];
+        if (c != allmask && (c == 0u || (c & (c - 1u)) != 0u)) return true;
+    }
+    return false;
+}
+
 bool all_finite(const double* p, int64_t n) {
     for (int64_t i = 0; i < n; ++i)
         if (!std::isfinite(p[i])) return false;
@@ -174,7 +184,7 @@ void choose_tiles(mcphy_engine* h) {
     h->spt = spt;
     int tpb = h->tpb_req ? h->tpb_req : 128;
     // every warp owns two staging buffers of step records in shared memory
-    const int per_warp = warp_smem_bytes(h->Kp, spt, int(real_size(h)));
+    const int per_warp = walk_smem_per_warp(h->Kp, spt, int(real_size(h)), h->walk_rows);
     const int max_warps = std::max(1, (200 * 1024) / per_warp);
     while (tpb / 32 > max_warps && tpb > 32) tpb -= 32;
     h->tpb = tpb;
@@ -196,9 +206,11 @@ int layout(mcphy_engine* h) {
     // of n leaves has n - 1 steps; work items of 32-site blocks
     h->max_J_hint = 0;
     h->items_hint = 0;
+    h->walk_rows = !h->force_general;
     for (const Inst& in : h->inst) {
         h->max_J_hint = std::max<int32_t>(h->max_J_hint, int32_t(in.leaf_nums.size()) - 1);
         h->items_hint += int64_t(h->C) * ((in.S + 31) / 32);
+        if (in.dense || in.ambig) h->walk_rows = false;
     }
     choose_tiles(h);
     const int SB = 32 * h->spt;
@@ -364,8 +376,9 @@ int layout(mcphy_engine* h) {
     int bps = 0;
     cudaError_t oe = tc ? occupancy_prune_tc(fmt, K, &bps)
                      : level ? occupancy_prune_level(h->prec == MCPHY_PREC_F64, Kp, h->tpb, h->max_J, &bps)
-                     : (h->prec == MCPHY_PREC_F64) ? occupancy_prune_f64(Kp, h->spt, h->tpb, &bps)
-                                                   : occupancy_prune_f32(Kp, h->spt, h->tpb, &bps);
+                     : (h->prec == MCPHY_PREC_F64)
+                         ? occupancy_prune_f64(Kp, h->spt, h->tpb, h->walk_rows, &bps)
+                         : occupancy_prune_f32(Kp, h->spt, h->tpb, h->walk_rows, &bps);
     if (oe != cudaSuccess || bps < 1) bps = 1;
     // work items per CTA at a time: one per warp (tree walk), one per CTA otherwise;
     // scratch columns: per warp (tree walk) or per 128-thread CTA (tensor cores)
@@ -439,13 +452,7 @@ int upload_data(mcphy_engine* h) {
         InstanceDesc& d = h->desc[i];
         // a code that is neither one state nor all states (or none) needs the
         // kernel's general bitmask path for this instance
-        d.ambig = 0;
-        if (!in.dense)
-            for (uint32_t c : in.codes)
-                if (c != allmask && (c == 0u || (c & (c - 1u)) != 0u)) {
-                    d.ambig = 1;
-                    break;
-                }
+        d.ambig = (!in.dense && in.ambig) ? 1 : 0;
         if (in.dense) {
             for (int64_t l = 0; l < d.n_leaf; ++l)
                 for (int64_t s = 0; s < d.S_pad; ++s) {
@@ -653,8 +660,8 @@ int run(mcphy_engine* h, bool want_grad) {
     if (h->inject == 1) h->inject = 0;
     CK(tc    ? launch_prune_tc(fmt, h->K, h->blocks, a, st)
        : h->sweep == MCPHY_SWEEP_LEVEL ? launch_prune_level(f64, h->Kp, h->blocks, h->tpb, a, st)
-       : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, a, st)
-             : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, a, st));
+       : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, h->walk_rows, a, st)
+             : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, h->walk_rows, a, st));
     if (h->timing) CK(cudaEventRecord(h->ev[2], st));
 
     ReduceArgs r{};
@@ -911,6 +918,8 @@ int mcphy_batch_set_data(mcphy_handle h, int64_t i, const double* x, int64_t nsi
         }
     }
     in.dense = !binary;
+    const bool was_ambig = in.ambig;
+    in.ambig = false;
     if (binary) {
         in.codes.assign(size_t(n_leaves * nsites), 0u);
         in.dvals.clear();
@@ -923,6 +932,7 @@ int mcphy_batch_set_data(mcphy_handle h, int64_t i, const double* x, int64_t nsi
                 in.codes[l * nsites + s] = c;
             }
         }
+        in.ambig = any_ambiguous(in.codes.data(), int64_t(in.codes.size()), K);
     } else {
         in.codes.clear();
         in.dvals.resize(size_t(n_leaves * nsites * K));
@@ -937,7 +947,8 @@ int mcphy_batch_set_data(mcphy_handle h, int64_t i, const double* x, int64_t nsi
             }
         }
     }
-    if (in.dense != was_dense) h->dirty |= DIRTY_LAYOUT;
+    // the tree-walk kernel (and its launch shape) depends on the kind of leaves
+    if (in.dense != was_dense || in.ambig != was_ambig) h->dirty |= DIRTY_LAYOUT;
     return MCPHY_OK;
 }
 
@@ -962,8 +973,10 @@ int mcphy_batch_set_codes(mcphy_handle h, int64_t i, const uint32_t* codes, int6
             in.has_data = false;
             return fail(h, MCPHY_ERR_ARG, "state bitmask has bits >= K");
         }
-    if (in.dense) h->dirty |= DIRTY_LAYOUT;
+    const bool ambig = any_ambiguous(codes, n_leaves * nsites, h->K);
+    if (in.dense || in.ambig != ambig) h->dirty |= DIRTY_LAYOUT;
     in.dense = false;
+    in.ambig = ambig;
     in.dvals.clear();
     in.codes.assign(codes, codes + n_leaves * nsites);
     return MCPHY_OK;
@@ -1198,8 +1211,13 @@ int mcphy_get_sweep(mcphy_handle h, int* sweep) {
 
 int mcphy_debug_inject(mcphy_handle h, int kind) {
     if (!h) return MCPHY_ERR_ARG;
-    if (kind < 0 || kind > 2) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
-    h->inject = kind;
+    if (kind < 0 || kind > 3) return fail(h, MCPHY_ERR_ARG, "unknown injection kind");
+    const bool general = kind == 3;
+    if (general != h->force_general) {
+        h->force_general = general;
+        h->dirty |= DIRTY_LAYOUT;
+    }
+    h->inject = general ? 0 : kind;
     return MCPHY_OK;
 }
 

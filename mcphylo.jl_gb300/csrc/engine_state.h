@@ -30,6 +30,7 @@ struct Inst {
     std::vector<int64_t> leaf_nums;
     bool dense = false;
     std::vector<uint32_t> codes;   // [leaf_row][S]
+    bool ambig = false;            // some code allows more than one but not all states
     std::vector<double> dvals;     // [leaf_row][S][K]
     std::vector<double> weights;   // [S] site-pattern weights; empty = every site once
     bool has_data = false;
@@ -61,6 +62,11 @@ struct mcphy_engine {
     int spt_req = 0, tpb_req = 0, sweep_req = 0;
     int spt = 1, tpb = 256, blocks = 0, sweep = 1;
     int32_t max_J_hint = 0;     // largest schedule, known before the layout (leaves - 1)
+    // tree walk: the row-code kernel when every leaf of every instance is a table-row
+    // code (no dense leaves, no partially ambiguous codes), else the general kernel;
+    // force_general is a test hook (mcphy_debug_inject kind 3)
+    bool walk_rows = false;
+    bool force_general = false;
     int64_t items_hint = 0;     // work items at 32-site blocks
 
     // layout

@@ -420,11 +420,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int li
 
 // Staging: chunk x of CH steps (records, and for code-leaf instances the leaf
 // codes of those steps) lives in buffer x & 1; one mbarrier per buffer.
-template <int KP, typename Real, int SPT>
+template <int KP, typename Real, int SPT, int CH_ = chunk_steps(KP, sizeof(Real))>
 struct Stage {
     static constexpr int BYTES = rec_bytes(KP, sizeof(Real));
     static constexpr int TIP = tip_bytes(KP, SPT);
-    static constexpr int CH = chunk_steps(KP, sizeof(Real));
+    static constexpr int CH = CH_;
     unsigned char* base;        // record buffer 0, record buffer 1, tip buffer 0, tip buffer 1
     uint64_t* bars;             // two mbarriers
     uint32_t parity;            // bit b: phase parity expected next on buffer b
@@ -1077,12 +1077,16 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
 constexpr int RY = 8;
 
 // Host-side launchers (defined per precision in kernels_f32.cu / kernels_f64.cu).
-cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, const PruneArgs& a,
+// rows: the row-code tree walk (kernels_walk.cuh), for handles whose leaves are all
+// table-row codes; else the general tree walk above.
+cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
                              cudaStream_t st);
-cudaError_t launch_prune_f64(int Kp, int spt, int blocks, int tpb, const PruneArgs& a,
+cudaError_t launch_prune_f64(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
                              cudaStream_t st);
-cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, int* blocks_per_sm);
-cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, int* blocks_per_sm);
+cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, bool rows, int* blocks_per_sm);
+cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, bool rows, int* blocks_per_sm);
+// shared memory of one warp of the tree walk
+int walk_smem_per_warp(int Kp, int spt, int real_bytes, bool rows);
 
 // Level-synchronous sweep for small trees (kernels_level.cu): a CTA of tpb threads
 // owns one 32-site work item at a time; its warps share the tree level by level.

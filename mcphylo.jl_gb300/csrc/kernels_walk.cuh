@@ -1,0 +1,344 @@
+// Tree walk for the common case: every leaf operand is a table-row code (no dense
+// leaf values, no partially ambiguous codes).  Same work items, records, staging,
+// scratch layout and arithmetic as prune_kernel (kernels.cuh), operation for
+// operation, so the two give the same bits; written so that no operand is copied
+// between register arrays:
+//   - a leaf operand is its row codes (one uint32 per site), looked up straight
+//     into the Down vector; an internal operand 1 is the previous step's partial,
+//     P_1 is applied to it where it lies and the product is written back in place;
+//   - the pre-order sweep is unrolled by two steps with two sets of prefetch
+//     registers used in turn (the next step's post-order operands load into one set
+//     while the other feeds the current step), and the pre-order partial of child 1
+//     is written where the next step reads it;
+//   - smaller staging chunks (at most 3 KB of records per buffer) so that more warps
+//     fit an SM.
+// (FelsensteinFunction, src/Likelihood/LikelihoodCalculator_Node.jl:3-114;
+// comb_sum_product_loop!, by_max!, bymax!, root_sum, turbo_mul!, mygemmturbo!:
+// src/Likelihood/VectorizedFunctions.jl:2-213.)
+#pragma once
+
+#include "kernels.cuh"
+
+namespace mcphy {
+
+// steps per staged chunk of the row-code walk: the largest power of two with at most
+// 3 KB of records per buffer (at least 1)
+__host__ __device__ constexpr int walk_chunk_steps(int kp, int real_bytes) {
+    return rec_bytes(kp, real_bytes) > 1536   ? 1
+           : rec_bytes(kp, real_bytes) > 768  ? 2
+           : rec_bytes(kp, real_bytes) > 384  ? 4
+           : rec_bytes(kp, real_bytes) > 192  ? 8
+                                              : 16;
+}
+__host__ __device__ constexpr int walk_warp_smem_bytes(int kp, int spt, int real_bytes) {
+    return (2 * walk_chunk_steps(kp, real_bytes) * (rec_bytes(kp, real_bytes) + tip_bytes(kp, spt)) +
+            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 + 127) /
+           128 * 128;
+}
+
+// Row codes of the warp's sites for one operand (staged in shared memory).
+template <int KP, int SPT>
+__device__ __forceinline__ void read_rows(const unsigned char* p, int lane, uint32_t (&c)[SPT]) {
+    using Code = typename CodeOf<KP>::type;
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) c[u] = uint32_t(reinterpret_cast<const Code*>(p)[u * 32 + lane]);
+}
+// D[u] = row c[u] of T (a leaf's Down vector: one column of the matrix, or the row
+// sums for a leaf with every state)
+template <int KP, int SPT, typename Real>
+__device__ __forceinline__ void lookup(const Real* T, const uint32_t (&c)[SPT], Real (&D)[SPT][KP]) {
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) ld_vec<KP>(T + c[u] * KP, D[u]);
+}
+// L = X * Y elementwise
+template <int KP, int SPT, typename Real>
+__device__ __forceinline__ void vmul(Real (&L)[SPT][KP], const Real (&X)[SPT][KP], const Real (&Y)[SPT][KP]) {
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) {
+        if constexpr (Pairs<Real, KP>::value) {
+#pragma unroll
+            for (int k = 0; k < KP; k += 2) mul2(X[u][k], X[u][k + 1], Y[u][k], Y[u][k + 1], L[u][k], L[u][k + 1]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < KP; ++k) L[u][k] = X[u][k] * Y[u][k];
+        }
+    }
+}
+
+template <int KP, typename Real, int SPT>
+__global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
+    constexpr int CH = walk_chunk_steps(KP, sizeof(Real));
+    using St = Stage<KP, Real, SPT, CH>;
+    constexpr int NS = stack_smem_slots(KP, SPT, sizeof(Real));
+    constexpr int SLOT = SPT * 32 * KP;             // Real elements per warp vector
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t gw = int64_t(blockIdx.x) * (blockDim.x >> 5) + wib;
+    Real* post = reinterpret_cast<Real*>(a.post) + gw * a.warp_stride;
+    Real* gstack = reinterpret_cast<Real*>(a.pre) + gw * a.pre_warp_stride;
+    const int C = a.C;
+    constexpr double LN2 = 0.6931471805599453094;
+
+    unsigned char* wbase = smem + size_t(wib) * walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)));
+    Real* sstack = reinterpret_cast<Real*>(wbase + 2 * CH * (St::BYTES + St::TIP));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
+                                                  NS * SLOT * sizeof(Real));
+    St st;
+    st.init(wbase, bars, lane, a.wait_limit, a.inject_timeout != 0);
+    if (lane == 0) fence_mbar_init();
+    __syncwarp();
+    // stack slot s: shared memory below NS, the warp's global column above
+    auto stack_ptr = [&](int s) -> Real* {
+        return s < NS ? sstack + s * SLOT : gstack + int64_t(s) * SLOT;
+    };
+
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(a.counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= a.n_items) break;
+        const int item = __ldg(a.queue + t);
+        const int2 it = __ldg(a.items + item);
+        const InstanceDesc d = a.inst[it.x];
+        const int r = it.y / d.n_blocks;
+        const int blk = it.y - r * d.n_blocks;
+        const int site0 = blk * (32 * SPT) + lane;
+        const double* pi_d = a.params + d.param_off + 2 * a.K * a.K + a.K + 1 + C;
+        const int J = d.J;
+
+        // site-pattern weights of the gradient terms, 0 past the last site
+        Real wtr[SPT];
+#pragma unroll
+        for (int u = 0; u < SPT; ++u)
+            wtr[u] = (site0 + 32 * u) < d.S ? Real(__ldg(a.weights + d.weight_off + site0 + 32 * u)) : Real(0);
+
+        st.src = a.recs + d.rec_off + size_t(r) * size_t(J) * St::BYTES;
+        st.tsrc = reinterpret_cast<const unsigned char*>(a.codes) + d.leaf_off +
+                  size_t(blk) * size_t(J) * St::TIP;
+        st.J = J;
+        st.Q = (J + CH - 1) / CH;
+        __syncwarp();
+        st.issue(0, lane);
+        if (st.Q > 1) st.issue(1, lane);
+
+        // ---------------- post-order sweep (logL)
+        uint32_t eacc[SPT];
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) eacc[u] = 0u;
+        double ll_lane = 0.0;
+        Real Lp[SPT][KP];          // the previous step's partial (operand 1 of the next step)
+        for (int j = 0; j < J; ++j) {
+            if (j % CH == 0 && !st.wait(j / CH)) break;
+            const unsigned char* rj = st.rec(j);
+            int h[8];
+            rec_header(rj, h);
+            Real D0[SPT][KP];
+            if (h[0] >= 0) {
+                Real A[SPT][KP];
+                read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
+                apply_t<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 0), A, D0);
+            } else {
+                uint32_t c[SPT];
+                read_rows<KP, SPT>(st.tip(j, 0), lane, c);
+                lookup<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 0), c, D0);
+            }
+            {
+                Real D1[SPT][KP];
+                if (h[1] >= 0) {
+                    apply_t<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 2), Lp, D1);
+                } else {
+                    uint32_t c[SPT];
+                    read_rows<KP, SPT>(st.tip(j, 1), lane, c);
+                    lookup<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 2), c, D1);
+                }
+                vmul<KP, SPT>(Lp, D0, D1);
+            }
+            rescale_warp<KP, Real, SPT>(Lp, eacc);
+            if (j + 1 < J) {
+                // the post-order column is only read back by the gradient sweep
+                if (a.want_grad) write_vec<KP, SPT>(post + int64_t(j) * SLOT, lane, Lp);
+                if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Lp);
+            } else {
+#pragma unroll
+                for (int u = 0; u < SPT; ++u) {
+                    Real lik = Real(0);
+#pragma unroll
+                    for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Lp[u][k], lik);
+                    const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
+                    const double v = log_site(lik) + double(ex) * LN2;
+                    const bool valid = (site0 + 32 * u) < d.S;
+                    const double w = valid ? __ldg(a.weights + d.weight_off + site0 + 32 * u) : 0.0;
+                    ll_lane += valid ? w * v : 0.0;
+                }
+            }
+            // chunk finished: refill its buffers with the chunk after next
+            if ((j + 1) % CH == 0 || j + 1 == J) {
+                __syncwarp();
+                if (j / CH + 2 < st.Q) st.issue(j / CH + 2, lane);
+            }
+        }
+        if (!st.ok) break;
+        ll_lane = warp_sum(ll_lane);
+        if (lane == 0) a.pll[item] = ll_lane;
+        if (!a.want_grad) continue;   // every issued chunk has been waited for
+
+        // ---------------- pre-order sweep (gradient)
+        // buffers hold chunks Q-1 and Q-2 (both waited for)
+        Real* pg = reinterpret_cast<Real*>(a.pgrad) + d.pgrad_off + int64_t(it.y) * d.n_branch;
+        int low = st.Q >= 2 ? st.Q - 2 : 0;   // lowest chunk waited for
+        Real pb[SPT][KP];                      // this step's own pre-order partial
+#pragma unroll
+        for (int u = 0; u < SPT; ++u)
+#pragma unroll
+            for (int k = 0; k < KP; ++k) pb[u][k] = Real(__ldg(pi_d + k));
+        if (lane == 0) {
+            // the first PF_DIST steps' post-order partials (later ones: from the records)
+            for (int q = 0; q < PF_DIST && q < CH && q < J; ++q) {
+                int hq[8];
+                rec_header(st.rec(J - 1 - q), hq);
+                for (int c = 0; c < 2; ++c)
+                    if (hq[c] >= 0) prefetch_l2(post + int64_t(hq[c]) * SLOT, SLOT * sizeof(Real));
+            }
+        }
+
+        // One pre-order step j with header h: its internal operands are in X0 / X1
+        // (loaded one step ahead); loads step j-1's into Y0 / Y1 and its header into
+        // hn.  False when a staging wait gave up.
+        auto pstep = [&](int j, const int (&h)[8], int (&hn)[8], Real (&X0)[SPT][KP], Real (&X1)[SPT][KP],
+                         Real (&Y0)[SPT][KP], Real (&Y1)[SPT][KP]) -> bool {
+            const unsigned char* rj = st.rec(j);
+            if (lane == 0) {
+                const int2 pf = rec_prefetch(rj);
+                if (pf.x >= 0) prefetch_l2(post + int64_t(pf.x) * SLOT, SLOT * sizeof(Real));
+                if (pf.y >= 0) prefetch_l2(post + int64_t(pf.y) * SLOT, SLOT * sizeof(Real));
+            }
+            if (h[3] >= 0) read_vec<KP, SPT>(stack_ptr(h[3]), lane, pb);   // else carried
+            uint32_t c0[SPT], c1[SPT];
+            if (h[0] < 0) read_rows<KP, SPT>(st.tip(j, 0), lane, c0);
+            if (h[1] < 0) read_rows<KP, SPT>(st.tip(j, 1), lane, c1);
+            // operands of the next step, one step ahead
+            if (j > 0) {
+                const int qn = (j - 1) / CH;
+                if (qn < low) {
+                    if (!st.wait(qn)) return false;
+                    low = qn;
+                }
+                rec_header(st.rec(j - 1), hn);
+                if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, Y0);
+                if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, Y1);
+            }
+            const Real* P0 = rec_mat_ptr<KP, Real>(rj, 0);
+            const Real* P1 = rec_mat_ptr<KP, Real>(rj, 2);
+            Real D0[SPT][KP], D1[SPT][KP];
+            if (h[0] >= 0) apply_t<KP, SPT>(P0, X0, D0);
+            else lookup<KP, SPT>(P0, c0, D0);
+            if (h[1] >= 0) apply_t<KP, SPT>(P1, X1, D1);
+            else lookup<KP, SPT>(P1, c1, D1);
+            Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
+            // wide state spaces: the gradient ratio's denominator pt_c . D_c =
+            // sum_k pb_k D0_k D1_k is the same for both children, computed once
+            constexpr bool kSharedDen = Pairs<Real, KP>::value;
+            Real den[kSharedDen ? SPT : 1];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                // pre-order partial at the top of branch c: mother's pre times the
+                // sibling's Down (turbo_mul!)
+                Real pt[SPT][KP];
+                vmul<KP, SPT>(pt, pb, c == 0 ? D1 : D0);
+                if constexpr (kSharedDen) {
+                    if (c == 0 && (h[4] >= 0 || h[5] >= 0)) {
+#pragma unroll
+                        for (int u = 0; u < SPT; ++u) {
+                            Real s0 = Real(0), s1 = Real(0);
+#pragma unroll
+                            for (int k = 0; k < KP; k += 2)
+                                fma2(pt[u][k], pt[u][k + 1], D0[u][k], D0[u][k + 1], s0, s1);
+                            den[u] = den_prep(s0 + s1);
+                        }
+                    }
+                }
+                if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
+                    Real dD[SPT][KP];
+                    const Real* dP = rec_mat_ptr<KP, Real>(rj, 2 * c + 1);
+                    if (h[c] >= 0) apply_t<KP, SPT>(dP, c == 0 ? X0 : X1, dD);
+                    else lookup<KP, SPT>(dP, c == 0 ? c0 : c1, dD);
+                    Real g = Real(0);
+#pragma unroll
+                    for (int u = 0; u < SPT; ++u) {
+                        if constexpr (kSharedDen) {
+                            Real n0 = Real(0), n1 = Real(0);
+#pragma unroll
+                            for (int k = 0; k < KP; k += 2)
+                                fma2(pt[u][k], pt[u][k + 1], dD[u][k], dD[u][k + 1], n0, n1);
+                            g = fma(wtr[u], den_apply(n0 + n1, den[u]), g);
+                        } else {
+                            const Real (&Dc)[SPT][KP] = c == 0 ? D0 : D1;
+                            Real num = Real(0), dn = Real(0);
+#pragma unroll
+                            for (int k = 0; k < KP; ++k) {
+                                num = fma(pt[u][k], dD[u][k], num);
+                                dn = fma(pt[u][k], Dc[u][k], dn);
+                            }
+                            g = fma(wtr[u], ratio(num, dn), g);
+                        }
+                    }
+                    gsum[c] = g;
+                }
+                if (h[c] >= 0) {
+                    uint32_t unused[SPT] = {};
+                    if (c == 1) {
+                        // child 1 is the next step: its pre-order partial is the next pb
+                        apply_tt<KP, SPT>(P1, pt, pb);
+                        rescale_warp<KP, Real, SPT>(pb, unused);
+                    } else {
+                        Real pbc[SPT][KP];
+                        apply_tt<KP, SPT>(P0, pt, pbc);
+                        rescale_warp<KP, Real, SPT>(pbc, unused);
+                        write_vec<KP, SPT>(stack_ptr(h[2]), lane, pbc);
+                    }
+                }
+            }
+            if (h[4] >= 0 || h[5] >= 0) {
+                // both children's warp sums in one shuffle tree: lanes 0-15 add child
+                // 0's terms, lanes 16-31 child 1's (the same pairs, in the same order,
+                // as a warp_sum of each)
+                const bool hi = (lane & 16) != 0;
+                Real v = hi ? gsum[1] : gsum[0];
+                v += __shfl_xor_sync(0xffffffffu, hi ? gsum[0] : gsum[1], 16);
+#pragma unroll
+                for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0 && h[4] >= 0) pg[h[4]] = v;
+                if (lane == 16 && h[5] >= 0) pg[h[5]] = v;
+            }
+            // chunk finished (descending): refill its buffers two chunks below
+            if (j % CH == 0) {
+                __syncwarp();
+                if (j / CH - 2 >= 0) st.issue(j / CH - 2, lane);
+            }
+            return true;
+        };
+
+        int h[8], hn[8];
+        rec_header(st.rec(J - 1), h);
+        Real Xa[SPT][KP], Xb[SPT][KP], Ya[SPT][KP], Yb[SPT][KP];
+        if (h[0] >= 0) read_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, Xa);
+        if (h[1] >= 0) read_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, Xb);
+        for (int j = J - 1; j >= 0;) {
+            if (!pstep(j, h, hn, Xa, Xb, Ya, Yb)) break;
+            if (--j < 0) break;
+            if (!pstep(j, hn, h, Ya, Yb, Xa, Xb)) break;
+            --j;
+        }
+        if (!st.ok) break;
+    }
+    if (!st.ok) {
+        // a bounded wait gave up: report, and let the copies this warp issued land
+        // (bounded as well) before its shared memory is released
+        if (lane == 0) atomicExch(a.counter + 1, 1);
+        mbar_wait(st.barrier(0), st.parity & 1u, a.wait_limit);
+        mbar_wait(st.barrier(1), (st.parity >> 1) & 1u, a.wait_limit);
+    }
+}
+
+}  // namespace mcphy

@@ -258,8 +258,8 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     a.plan = static_cast<const int32_t*>(h->d_plan.p);
     a.max_J = h->max_J;
     NA_CK(h->sweep == MCPHY_SWEEP_LEVEL ? launch_prune_level(f64, h->Kp, int(blocks), h->tpb, a, st)
-          : f64 ? launch_prune_f64(h->Kp, h->spt, int(blocks), h->tpb, a, st)
-                : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, a, st));
+          : f64 ? launch_prune_f64(h->Kp, h->spt, int(blocks), h->tpb, h->walk_rows, a, st)
+                : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, h->walk_rows, a, st));
 
     ReduceArgs r{};
     r.inst = b.inst;

@@ -1,11 +1,13 @@
-// Launch and occupancy of the tree-walk sweep prune_kernel<KP, Real, SPT>, shared by
-// the FP32 (kernels_f32.cu) and FP64 (kernels_f64.cu) translation units.
+// Launch and occupancy of the tree-walk sweeps prune_kernel<KP, Real, SPT> (any
+// leaves) and prune_rows_kernel<KP, Real, SPT> (table-row leaf codes), shared by the
+// FP32 (kernels_f32.cu) and FP64 (kernels_f64.cu) translation units.
 #pragma once
 
 #include <algorithm>
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "kernels_walk.cuh"
 #include "launch_attr.h"
 
 namespace mcphy {
@@ -18,42 +20,49 @@ __host__ __device__ constexpr int walk_spt_max(int kp, int real_bytes) {
 
 template <typename Real>
 struct PruneLaunch {
-    template <int KP, int SPT>
+    template <int KP, int SPT, bool ROWS>
+    static const void* kernel() {
+        if constexpr (ROWS) return reinterpret_cast<const void*>(&prune_rows_kernel<KP, Real, SPT>);
+        else return reinterpret_cast<const void*>(&prune_kernel<KP, Real, SPT>);
+    }
+    template <int KP, int SPT, bool ROWS>
     static SmemAllowance& allowance() {
         static SmemAllowance a;
         return a;
     }
-    template <int KP, int SPT>
+    template <int KP, int SPT, bool ROWS>
     static cudaError_t allow(int smem) {
-        return raise_smem(allowance<KP, SPT>(), smem, [](int bytes) {
-            return cudaFuncSetAttribute(prune_kernel<KP, Real, SPT>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        return raise_smem(allowance<KP, SPT, ROWS>(), smem, [](int bytes) {
+            return cudaFuncSetAttribute(kernel<KP, SPT, ROWS>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        bytes);
         });
     }
-    template <int KP, int SPT>
+    template <int KP, int SPT, bool ROWS>
     static int smem_of(int tpb) {
-        return (tpb / 32) * warp_smem_bytes(KP, SPT, int(sizeof(Real)));
+        return (tpb / 32) * (ROWS ? walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)))
+                                  : warp_smem_bytes(KP, SPT, int(sizeof(Real))));
     }
-    template <int KP, int SPT>
+    template <int KP, int SPT, bool ROWS>
     static cudaError_t go(int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
-        const int smem = smem_of<KP, SPT>(tpb);
-        cudaError_t e = allow<KP, SPT>(smem);
+        const int smem = smem_of<KP, SPT, ROWS>(tpb);
+        cudaError_t e = allow<KP, SPT, ROWS>(smem);
         if (e != cudaSuccess) return e;
-        prune_kernel<KP, Real, SPT><<<blocks, tpb, smem, st>>>(a);
+        if constexpr (ROWS) prune_rows_kernel<KP, Real, SPT><<<blocks, tpb, smem, st>>>(a);
+        else prune_kernel<KP, Real, SPT><<<blocks, tpb, smem, st>>>(a);
         return cudaGetLastError();
     }
-    template <int KP, int SPT>
+    template <int KP, int SPT, bool ROWS>
     static cudaError_t occ(int tpb, int* bps) {
-        const int smem = smem_of<KP, SPT>(tpb);
+        const int smem = smem_of<KP, SPT, ROWS>(tpb);
         // the largest block a later launch may use (8 warps), so that launches need
         // not raise it again; where that does not fit, the block asked for
-        cudaError_t e = allow<KP, SPT>(std::max(smem, smem_of<KP, SPT>(256)));
+        cudaError_t e = allow<KP, SPT, ROWS>(std::max(smem, smem_of<KP, SPT, ROWS>(256)));
         if (e != cudaSuccess) {
             cudaGetLastError();
-            e = allow<KP, SPT>(smem);
+            e = allow<KP, SPT, ROWS>(smem);
         }
         if (e != cudaSuccess) return e;
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_kernel<KP, Real, SPT>, tpb, smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, kernel<KP, SPT, ROWS>(), tpb, smem);
     }
 
     // f(integral_constant KP, integral_constant SPT) for the instantiated shapes;
@@ -76,14 +85,17 @@ struct PruneLaunch {
             default: return cudaErrorInvalidValue;
         }
     }
-    static cudaError_t launch(int Kp, int spt, int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
+    static cudaError_t launch(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
+                              cudaStream_t st) {
         return dispatch(Kp, spt, [&](auto kp, auto s) {
-            return go<decltype(kp)::value, decltype(s)::value>(blocks, tpb, a, st);
+            constexpr int K_ = decltype(kp)::value, S_ = decltype(s)::value;
+            return rows ? go<K_, S_, true>(blocks, tpb, a, st) : go<K_, S_, false>(blocks, tpb, a, st);
         });
     }
-    static cudaError_t occupancy(int Kp, int spt, int tpb, int* bps) {
+    static cudaError_t occupancy(int Kp, int spt, int tpb, bool rows, int* bps) {
         return dispatch(Kp, spt, [&](auto kp, auto s) {
-            return occ<decltype(kp)::value, decltype(s)::value>(tpb, bps);
+            constexpr int K_ = decltype(kp)::value, S_ = decltype(s)::value;
+            return rows ? occ<K_, S_, true>(tpb, bps) : occ<K_, S_, false>(tpb, bps);
         });
     }
 };

@@ -244,11 +244,13 @@ double orc_felsenstein_ll(i64 N, const i64* post, const i64* cptr, const i64* ci
 }
 
 /* FelsensteinFunction, gradient form (LikelihoodCalculator_Node.jl:3-78).
- * grv has N-1 entries indexed by num-1.  Returns ll. */
+ * grv has N-1 entries indexed by num-1.  Returns ll.  When gabs is not NULL it
+ * receives, per entry, the sum of |gradi / col| over sites and rates: the size of
+ * the terms that cancel in the entry (its condition number is gabs / |grv|). */
 double orc_felsenstein_grad(i64 N, const i64* post, const i64* cptr, const i64* cidx,
                             const i64* mother, double* data, double* Down,
                             const double* pi, const double* P, const double* ptg,
-                            i64 K, i64 S, i64 C, double* grv) {
+                            i64 K, i64 S, i64 C, double* grv, double* gabs) {
     double ll = orc_felsenstein_ll(N, post, cptr, cidx, data, Down, pi, P, K, S, C);
     size_t nelem = (size_t)(K * S * C * N);
     double* pre = (double*)malloc(sizeof(double) * nelem);
@@ -309,14 +311,16 @@ double orc_felsenstein_grad(i64 N, const i64* post, const i64* cptr, const i64* 
         }
 
         /* res = sum_{site, rate} gradi / col, serial in the reference's order (:59-67) */
-        double res = 0.0;
+        double res = 0.0, ares = 0.0;
         for (i64 j = 0; j < S; ++j)
             for (i64 r = 0; r < C; ++r) {
                 double col = 0.0;
                 for (i64 k = 0; k < K; ++k) col += data[D4(k, j, r, n)] * pre[D4(k, j, r, n)];
                 res += gradi[j + S * r] / col;
+                ares += fabs(gradi[j + S * r] / col);
             }
         grv[n] = res;
+        if (gabs) gabs[n] = ares;
 
         if (cptr[num] - cptr[num - 1] > 0) bymax_pre(pre, num, K, S, C, maxi);
         (void)root;
@@ -355,7 +359,7 @@ double orc_gradlogpdf(i64 N, const i64* post, const i64* cptr, const i64* cidx,
                       const i64* mother, const i64* leaf_nums, i64 nleaf, const double* x,
                       const double* U, const double* D, const double* Uinv, double mu,
                       const double* pi, const double* rates, const double* blv,
-                      i64 K, i64 S, i64 C, double* grad) {
+                      i64 K, i64 S, i64 C, double* grad, double* gabs) {
     size_t nelem = (size_t)(K * S * C * N);
     size_t np = (size_t)(K * K * C * (N - 1));
     double* data = (double*)malloc(sizeof(double) * nelem);
@@ -367,7 +371,7 @@ double orc_gradlogpdf(i64 N, const i64* post, const i64* cptr, const i64* cidx,
     orc_parallel_transition_prob(U, D, Uinv, rates, C, mu, blv, N - 1, K, P);
     orc_transition_grad(U, D, Uinv, rates, C, mu, blv, N - 1, K, dP);
     double ll = orc_felsenstein_grad(N, post, cptr, cidx, mother, data, Down, pi, P, dP,
-                                     K, S, C, grad);
+                                     K, S, C, grad, gabs);
     free(data);
     free(Down);
     free(P);

@@ -63,7 +63,7 @@ def lib():
                                  pd, pd, pd, i64, i64, i64]
         L.orc_gradlogpdf.restype = dbl
         L.orc_gradlogpdf.argtypes = [i64, pi64, pi64, pi64, pi64, pi64, i64, pd, pd, pd, pd,
-                                     dbl, pd, pd, pd, i64, i64, i64, pd]
+                                     dbl, pd, pd, pd, i64, i64, i64, pd, pd]
         L.orc_parallel_transition_prob.restype = None
         L.orc_parallel_transition_prob.argtypes = [pd, pd, pd, pd, i64, dbl, pd, i64, i64, pd]
         L.orc_transition_grad.restype = None
@@ -434,17 +434,22 @@ def logpdf(root, x, pi, model_out, rates, blv=None) -> float:
                             _pd(pi), _pd(rates), _pd(blv), K, S, C)
 
 
-def gradlogpdf(root, x, pi, model_out, rates, blv=None):
-    """gradlogpdf(d::PhyloDist, x) (Phylodist.jl:124-138) -> (ll, grad[N-1])."""
+def gradlogpdf(root, x, pi, model_out, rates, blv=None, with_scale=False):
+    """gradlogpdf(d::PhyloDist, x) (Phylodist.jl:124-138) -> (ll, grad[N-1]).
+
+    with_scale=True also returns, per entry, the sum over sites and rates of the
+    absolute values of the terms the entry adds up (the entry's condition number is
+    scale / |grad|)."""
     (N, post, cptr, cidx, mother, leaf_nums, xf, Uf, Dd, Uif, mu, rates, blv, K, S,
      C) = _prep(root, x, model_out, rates, blv)
     pi = np.ascontiguousarray(pi, dtype=np.float64)
     grad = np.zeros(N - 1, dtype=np.float64)
+    scale = np.zeros(N - 1, dtype=np.float64) if with_scale else None
     ll = lib().orc_gradlogpdf(N, _p64(post), _p64(cptr), _p64(cidx), _p64(mother),
                               _p64(leaf_nums), len(leaf_nums), _pd(xf), _pd(Uf), _pd(Dd),
                               _pd(Uif), mu, _pd(pi), _pd(rates), _pd(blv), K, S, C,
-                              _pd(grad))
-    return ll, grad
+                              _pd(grad), _pd(scale) if with_scale else None)
+    return (ll, grad, scale) if with_scale else (ll, grad)
 
 
 def transition_matrices(model_out, rates, blv):

@@ -1,0 +1,164 @@
+"""Parity with the oracle at the benchmark configurations' own sizes.
+
+Each configuration's workload generator (mcphylo_gb300.simulate) builds the full
+problem; the engine evaluates it and the oracle (the reference's loops, FP64)
+evaluates the same inputs -- the whole alignment where it finishes in seconds,
+otherwise a site window of the full tree (all sites of the window, every instance
+of a batch):
+
+  1. restriction, 32 taxa x 1,000 sites, K=2, C=1                (whole)
+  2. GTR+G4, 128 taxa x 100,000 weighted patterns, K=4            (whole; the oracle
+     has no weights, so it sees every pattern repeated weight times, in windows)
+  3. restriction+G4, 512-taxon birth-death tree, 20,000 sites     (2,000-site window)
+  4. 256 HKY+G4 instances, 16-1,024 taxa, 500-50,000 sites         (every instance on
+     its first <= 2,000 sites, all in one batched launch)
+  5. 20-state GTR+G4, 256 taxa x 50,000 sites                     (500-site window)
+
+Bounds: FP64 logL 1e-12 relative, gradient 1e-10 of max|g| (per instance); FP32
+logL 1e-6 relative, gradient entries 1e-4 relative to max(|g_i|, 1e-2 max|g|), and
+1e-4 relative with no floor on every entry whose condition number is at most 1000.
+The condition number of entry i is sum_{site,rate} |term| / |g_i| (from the
+oracle): an entry adds up per-site terms that partly cancel, and rounding in any
+evaluation, the oracle's own included, scales with the size of those terms, not with
+|g_i|.  Each test prints the worst entry without a floor next to the bounds.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gpu_cases import (F32_G_FLOOR, F32_G_RTOL, F32_LL_RTOL, F64_G_FLOOR, F64_G_RTOL, F64_RTOL,
+                       assert_grad_close)
+from oracle import pyoracle as O
+
+import mcphylo_gb300 as mp
+from mcphylo_gb300 import simulate
+
+pytestmark = pytest.mark.gpu
+
+KAPPA_F32 = 1000.0      # FP32 entries held to 1e-4 without a floor
+_cache = {}
+
+
+def _one(key, make):
+    if key not in _cache:
+        _cache[key] = make()
+    return _cache[key]
+
+
+def window(inst, s1, s0=0):
+    return simulate.Instance(inst.tree, inst.parent, inst.blen, inst.leaf_nums,
+                             np.ascontiguousarray(inst.codes[:, s0:s1]), inst.U, inst.D,
+                             inst.Uinv, inst.mu, inst.pi, inst.rates)
+
+
+def oracle_scaled(inst, weights=None, cols=20_000):
+    """(ll, grad, scale) of the oracle; with integer weights, on the alignment whose
+    pattern s is repeated weights[s] times, in windows of about `cols` columns
+    (logL, gradient and scale are sums over columns)."""
+    t = O.tree_from_parent(inst.parent, inst.blen)
+    model = (inst.U, inst.D, inst.Uinv, inst.mu)
+    if weights is None:
+        return O.gradlogpdf(t, inst.tensor(), inst.pi, model, inst.rates, with_scale=True)
+    w = np.asarray(weights, dtype=np.int64)
+    step = max(1, int(cols / max(1.0, float(w.mean()))))   # patterns per window
+    ll, g, a = 0.0, np.zeros(inst.N - 1), np.zeros(inst.N - 1)
+    for s0 in range(0, inst.S, step):
+        s1 = min(inst.S, s0 + step)
+        sub = window(inst, s1, s0)
+        sub.codes = np.repeat(sub.codes, w[s0:s1], axis=1)
+        l_, g_, a_ = O.gradlogpdf(t, sub.tensor(), inst.pi, model, inst.rates, with_scale=True)
+        ll, g, a = ll + l_, g + g_, a + a_
+    return ll, g, a
+
+
+def engine_for(insts, precision, weights=None):
+    e = mp.Engine(insts[0].K, len(insts[0].rates), precision, n_instances=len(insts))
+    for i, inst in enumerate(insts):
+        e.set_tree(inst.parent, inst.blen, i)
+        e.set_codes(inst.codes, inst.leaf_nums, i)
+        e.set_model(inst.U, inst.D, inst.Uinv, inst.mu, inst.pi, inst.rates, i)
+        if weights is not None:
+            e.set_weights(np.asarray(weights, dtype=float), i)
+    return e
+
+
+def check(name, precision, ll, g, refs, off):
+    """refs: one (ll, grad, scale) of the oracle per instance; off: packed offsets."""
+    ll = np.atleast_1d(ll)
+    llo = np.array([r[0] for r in refs])
+    go = np.concatenate([r[1] for r in refs])
+    a = np.concatenate([r[2] for r in refs])
+    ll_err = float(np.max(np.abs(ll - llo) / np.abs(llo)))
+    floored = 0.0
+    for i, r in enumerate(refs):   # the norm-wise / floored bounds use each instance's max|g|
+        sl = slice(off[i], off[i + 1])
+        if precision == "f64":
+            floored = max(floored, assert_grad_close(g[sl], r[1], F64_G_RTOL, F64_G_FLOOR))
+        else:
+            floored = max(floored, assert_grad_close(g[sl], r[1], F32_G_RTOL, F32_G_FLOOR))
+    kappa = a / np.maximum(np.abs(go), 1e-300)
+    rel = np.abs(g - go) / np.maximum(np.abs(go), 1e-300)
+    held = kappa <= KAPPA_F32
+    print(f"\n[{name} {precision}] {len(refs)} instance(s): logL rel {ll_err:.2e} | grad: floored "
+          f"{floored:.2e}, unfloored max {float(rel.max()):.2e} (kappa {float(kappa[rel.argmax()]):.3g}), "
+          f"kappa<={KAPPA_F32:g}: {int(held.sum())}/{len(g)} entries, max "
+          f"{float(rel[held].max()) if held.any() else 0.0:.2e}")
+    if precision == "f64":
+        assert ll_err <= F64_RTOL, (name, ll_err)
+    else:
+        assert ll_err <= F32_LL_RTOL, (name, ll_err)
+        assert not held.any() or float(rel[held].max()) <= F32_G_RTOL, (name, float(rel[held].max()))
+
+
+def run(name, precision, insts, refs, weights=None):
+    e = engine_for(insts, precision, weights)
+    ll, g = e.logpdf_grad()
+    off = e.grad_offsets()
+    e.close()
+    check(name, precision, ll, g, refs, off)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_config1_restriction_whole(built_lib, precision):
+    inst = _one("c1", lambda: simulate.restriction_small())
+    run("config1", precision, [inst], [_one("c1o", lambda: oracle_scaled(inst))])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_config2_gtr_gamma_whole_weighted(built_lib, precision):
+    inst = _one("c2", lambda: simulate.gtr_gamma())
+    refs = [_one("c2o", lambda: oracle_scaled(inst, inst.weights))]
+    run("config2", precision, [inst], refs, inst.weights)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_config3_birth_death_full_tree(built_lib, precision):
+    inst = _one("c3w", lambda: window(simulate.restriction_gamma_bd(), 2000))
+    run("config3", precision, [inst], [_one("c3o", lambda: oracle_scaled(inst))])
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_config4_every_batched_instance(built_lib, precision):
+    wins = _one("c4w", lambda: [window(b, min(b.S, 2000)) for b in simulate.hky_batch(
+        seed=4, workers=min(16, os.cpu_count() or 1))])
+    refs = _one("c4o", lambda: [oracle_scaled(w) for w in wins])
+    run("config4", precision, wins, refs)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "tf32", "bf16"])
+def test_config5_protein_full_tree(built_lib, precision):
+    inst = _one("c5w", lambda: window(simulate.protein_gamma(), 500))
+    ref = _one("c5o", lambda: oracle_scaled(inst))
+    if precision in ("f64", "f32"):
+        run("config5", precision, [inst], [ref])
+        return
+    # tensor-core operands: TF32 keeps 10 mantissa bits, BF16 7
+    e = engine_for([inst], precision)
+    ll, g = e.logpdf_grad()
+    e.close()
+    ll_tol, g_tol = {"tf32": (5e-4, 5e-3), "bf16": (5e-3, 5e-2)}[precision]
+    ll_err = abs(ll - ref[0]) / abs(ref[0])
+    g_err = float(np.max(np.abs(g - ref[1])) / np.max(np.abs(ref[1])))
+    print(f"\n[config5 {precision}] logL rel {ll_err:.2e} | grad {g_err:.2e} of max|g|")
+    assert ll_err <= ll_tol and g_err <= g_tol
