@@ -378,6 +378,19 @@ def run_nuts(args):
             per_eval = spent["s"] / max(spent["n"], 1)
             res[prec]["host_seconds"] = max(
                 ch.seconds - per_eval * (ch.grad_evals + ch.logf_evals), 0.0)
+            # one posterior evaluation as the sampler calls it (wall, host API with the
+            # prior) against the device time of the engine's evaluation (CUDA events)
+            res[prec]["ms_per_eval_call"] = 1e3 * per_eval
+            e = post.eng
+            e.enable_timing(True)
+            dev = []
+            for _ in range(30):
+                e.logpdf_grad()
+                t3 = e.timing()
+                dev.append(t3["build_p_ms"] + t3["prune_ms"] + t3["reduce_ms"])
+            e.enable_timing(False)
+            res[prec]["device_ms_per_grad_eval"] = statistics.median(dev[5:])
+            res[prec]["launches_per_eval"] = e.counts()["launches"]
     clocks = clk.summary()
     # CPU: the oracle drives the same sampler.  With the same seed its chain retraces
     # the FP64 engine's (the decisions agree), so where a full run does not fit the

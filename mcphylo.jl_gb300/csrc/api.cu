@@ -353,6 +353,8 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_pll, sizeof(double) * size_t(h->n_items)))) return rc;
     if ((rc = ensure(h, h->d_out, sizeof(double) * size_t(h->M + h->total_branch)))) return rc;
     if ((rc = ensure(h, h->d_counter, 256))) return rc;
+    // [0] work counter, [1] error flag, [2] finished CTAs of a single-launch evaluation
+    CK(cudaMemset(h->d_counter.p, 0, 256));
     const size_t code_bytes = (Kp <= 8) ? 1 : 4;
     if ((rc = ensure(h, h->d_codes, code_bytes * size_t(h->leaf_elems)))) return rc;
     if ((rc = ensure(h, h->d_leafcodes, code_bytes * size_t(std::max<int64_t>(h->leafcode_elems, 64)))))
@@ -607,12 +609,60 @@ int prepare(mcphy_engine* h) {
     return MCPHY_OK;
 }
 
+// Kernel launches of one evaluation.
+int launches_per_eval(const mcphy_engine* h) {
+    if (tc_fmt(h) < 0 && h->sweep == MCPHY_SWEEP_LEVEL) return 1;
+    return 2 + reduce_launches(h->n_split);
+}
+
+// Small problems (level sweep): the whole evaluation as one launch -- records built
+// per CTA, level sweep, reduction by the last CTA; results land in d_out.
+int run_fused(mcphy_engine* h, bool want_grad) {
+    cudaStream_t st = h->stream;
+    if (h->timing) CK(cudaEventRecord(h->ev[1], st));   // no separate record build
+    PruneArgs a{};
+    a.inst = static_cast<const InstanceDesc*>(h->d_desc.p);
+    a.items = static_cast<const int2*>(h->d_items.p);
+    a.queue = static_cast<const int32_t*>(h->d_queue.p);
+    a.n_items = int32_t(h->n_items);
+    a.counter = static_cast<int32_t*>(h->d_counter.p);
+    a.codes = h->d_codes.p;
+    a.dense = h->d_dense.p;
+    a.params = static_cast<const double*>(h->d_params.p);
+    a.pgrad = h->d_pgrad.p;
+    a.pll = static_cast<double*>(h->d_pll.p);
+    a.K = h->K;
+    a.C = h->C;
+    a.want_grad = want_grad ? 1 : 0;
+    a.wait_limit = kWaitLimit;
+    a.lcodes = h->d_leafcodes.p;
+    a.sched = static_cast<const SchedNode*>(h->d_sched.p);
+    a.weights = static_cast<const double*>(h->d_weights.p);
+    a.plan = static_cast<const int32_t*>(h->d_plan.p);
+    a.max_J = h->max_J;
+    a.blen = static_cast<const double*>(h->d_blen.p);
+    a.out = static_cast<double*>(h->d_out.p);
+    a.n_inst = int32_t(h->M);
+    a.n_split = h->n_split;
+    a.total_branch = h->total_branch;
+    if (h->inject == 1) h->inject = 0;   // no staging waits to make run out
+    CK(launch_prune_level_fused(h->prec == MCPHY_PREC_F64, h->Kp, h->blocks, h->tpb, a, st));
+    if (h->timing) {
+        CK(cudaEventRecord(h->ev[2], st));
+        CK(cudaEventRecord(h->ev[3], st));
+    }
+    h->counts[0] = 1;
+    h->counts[1] = h->units;
+    return MCPHY_OK;
+}
+
 // Enqueues P build, fused sweep and reduction on the handle's stream; results land
 // in d_out = [ll (M) | grad (total_branch)].
 int run(mcphy_engine* h, bool want_grad) {
     const bool f64 = h->prec == MCPHY_PREC_F64;
     cudaStream_t st = h->stream;
     if (h->timing) CK(cudaEventRecord(h->ev[0], st));
+    if (tc_fmt(h) < 0 && h->sweep == MCPHY_SWEEP_LEVEL) return run_fused(h, want_grad);
 
     BuildRecArgs b{};
     b.inst = static_cast<const InstanceDesc*>(h->d_desc.p);
@@ -752,7 +802,7 @@ int eval_host(mcphy_engine* h, double* ll, double* grad, bool want_grad) {
         cudaGraphExec_t ex = nullptr;
         if ((rc = graph_for(h, want_grad, false, &ex))) return rc;
         CK(cudaGraphLaunch(ex, h->stream));
-        h->counts[0] = 2 + reduce_launches(h->n_split);
+        h->counts[0] = launches_per_eval(h);
         h->counts[1] = h->units;
     } else {
         if ((rc = enqueue_eval(h, want_grad))) return rc;
@@ -774,7 +824,7 @@ int run_device(mcphy_engine* h, bool want_grad) {
         int rc;
         if ((rc = graph_for(h, want_grad, true, &ex))) return rc;
         CK(cudaGraphLaunch(ex, h->stream));
-        h->counts[0] = 2 + reduce_launches(h->n_split);
+        h->counts[0] = launches_per_eval(h);
         h->counts[1] = h->units;
         return MCPHY_OK;
     }
@@ -1349,8 +1399,9 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
         float t = 1e30f;
         for (int rep = 0; rep < 3 && rc == MCPHY_OK; ++rep) {
             rc = eval_host(h, ll.data(), g.data(), true);
-            // the sweep and the reduction (item counts differ between launch shapes)
-            if (rep > 0) t = std::min(t, h->ms[1] + h->ms[2]);
+            // the whole evaluation (the single-launch level sweep builds its records
+            // itself; item counts differ between launch shapes)
+            if (rep > 0) t = std::min(t, h->ms[0] + h->ms[1] + h->ms[2]);
         }
         if (rc) break;
         if (t < best) {

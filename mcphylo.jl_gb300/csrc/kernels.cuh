@@ -113,6 +113,13 @@ struct PruneArgs {
     const double* weights;    // site-pattern weights per instance [S_pad], 0 past S
     const int32_t* plan;      // level plans (level-synchronous sweep), per instance at plan_off
     int32_t max_J;            // largest schedule (level-synchronous sweep: shared-memory layout)
+    // single-launch level sweep only: it builds its records from the FP64 parameters
+    // and branch lengths, and its last CTA reduces every item's partials into out
+    const double* blen;       // packed branch lengths
+    double* out;              // [n_inst + total_branch]: ll per instance, then gradients
+    int32_t n_inst;
+    int32_t n_split;          // item ranges of the reduction (its order is the regular one's)
+    int64_t total_branch;
 };
 
 // ---------------------------------------------------------------- tensor-core records
@@ -983,26 +990,15 @@ prune_kernel(const PruneArgs a) {
 // thread also writes the header.
 __host__ __device__ constexpr int rec_row_threads(int kp) { return kp >= 8 ? kp : 1; }
 
+// Part (child c, rows s0, s0 + R, ..) of the record of schedule step j (node sn) of
+// instance d for rate r, written at rec; the (c == 0, s0 == 0) part also writes the
+// header.  Shared by the global record build and the fused small-problem sweep, so
+// both give the same bits.
 template <typename Real>
-__global__ void build_records_kernel(const BuildRecArgs a) {
-    const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const int K = a.K, Kp = a.Kp, C = a.C;
-    const int R = rec_row_threads(Kp);
-    if (tid == 0 && a.counter) {
-        a.counter[0] = 0;
-        a.counter[1] = 0;
-    }
-    if (tid >= int64_t(a.n_steps) * 2 * C * R) return;
-    const int s0 = int(tid % R);
-    const int64_t u = tid / R;
-    const int r = int(u % C);
-    const int c = int((u / C) % 2);
-    const int2 sj = a.steps[u / (2 * C)];
-    const InstanceDesc& d = a.inst[sj.x];
-    const int j = sj.y;
-    const SchedNode sn = a.sched[d.sched_off + j];
-    const int bytes = rec_bytes(Kp, sizeof(Real));
-    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(bytes);
+__device__ __forceinline__ void build_record_part(unsigned char* rec, const SchedNode& sn,
+                                                  const SchedNode* sched, const InstanceDesc& d,
+                                                  const double* params, const double* blen, int j,
+                                                  int K, int Kp, int r, int c, int s0, int R) {
     if (c == 0 && s0 == 0) {
         int* hd = reinterpret_cast<int*>(rec);
         hd[0] = sn.op[0];
@@ -1015,7 +1011,7 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
         hd[7] = sn.fpush;
         // internal operands of the step PF_DIST later in the pre-order sweep
         const int jp = j - PF_DIST;
-        const SchedNode snp = a.sched[d.sched_off + (jp >= 0 ? jp : 0)];
+        const SchedNode snp = sched[jp >= 0 ? jp : 0];
         hd[8] = (jp >= 0 && snp.op[0] >= 0) ? snp.op[0] : -1;
         hd[9] = (jp >= 0 && snp.op[1] >= 0) ? snp.op[1] : -1;
         hd[10] = 0;
@@ -1036,12 +1032,12 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
         }
         return;
     }
-    const double* U = a.params + d.param_off;
+    const double* U = params + d.param_off;
     const double* Dv = U + K * K;
     const double* Uinv = Dv + K;
     const double mu = Uinv[K * K];
     const double rate = Uinv[K * K + 1 + r];
-    const double t = a.blen[d.blen_off + b];
+    const double t = blen[d.blen_off + b];
     double e[32], de[32];
     if (s0 < K)
         for (int m = 0; m < K; ++m) {
@@ -1071,6 +1067,28 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     }
 }
 
+template <typename Real>
+__global__ void build_records_kernel(const BuildRecArgs a) {
+    const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int K = a.K, Kp = a.Kp, C = a.C;
+    const int R = rec_row_threads(Kp);
+    if (tid == 0 && a.counter) {
+        a.counter[0] = 0;
+        a.counter[1] = 0;
+    }
+    if (tid >= int64_t(a.n_steps) * 2 * C * R) return;
+    const int s0 = int(tid % R);
+    const int64_t u = tid / R;
+    const int r = int(u % C);
+    const int c = int((u / C) % 2);
+    const int2 sj = a.steps[u / (2 * C)];
+    const InstanceDesc& d = a.inst[sj.x];
+    const int j = sj.y;
+    const SchedNode sn = a.sched[d.sched_off + j];
+    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(rec_bytes(Kp, sizeof(Real)));
+    build_record_part<Real>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, r, c, s0, R);
+}
+
 // ---------------------------------------------------------------- reduction
 // Per (instance, branch) FP64 sums of the item partials, in two passes with a
 // fixed summation order (kernels_common.cu).
@@ -1095,6 +1113,11 @@ bool level_supported(int Kp);
 int level_smem_bytes(int Kp, int real_bytes, int max_J, int warps);
 cudaError_t launch_prune_level(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
                                cudaStream_t st);
+// The whole evaluation of a small problem in one launch: records built per CTA in
+// shared memory, the level sweep, and the fixed-order reduction by the last CTA
+// (counter[2] counts finished CTAs and is left at zero).  Results land in a.out.
+cudaError_t launch_prune_level_fused(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
+                                     cudaStream_t st);
 cudaError_t occupancy_prune_level(bool f64, int Kp, int tpb, int max_J, int* blocks_per_sm);
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st);
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st);

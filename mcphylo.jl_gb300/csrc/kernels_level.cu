@@ -51,7 +51,13 @@ int level_smem_bytes(int kp, int real_bytes, int max_J, int warps) {
     return LevelSmem(kp, real_bytes, max_J, warps).total;
 }
 
-template <int KP, typename Real>
+// FUSED: the single-launch form for small problems -- each CTA builds its item's
+// records (rate r) in shared memory from the FP64 parameters and branch lengths
+// (build_record_part, the arithmetic of the global record build), and the last CTA
+// to finish reduces every item's partials in a fixed order (the regular reduction's
+// sums per instance and branch over items in item order), so an evaluation is one
+// kernel.
+template <int KP, typename Real, bool FUSED>
 __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) {
     constexpr int RB = rec_bytes(KP, sizeof(Real));
     constexpr int SLOT = 32 * KP;   // Reals of one step's vector (32 sites)
@@ -70,6 +76,10 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
     int32_t* splan = reinterpret_cast<int32_t*>(smem + lay.plan);
     Code* scode = reinterpret_cast<Code*>(smem + lay.code);
     const int C = a.C;
+    if constexpr (FUSED) {
+        // this evaluation has no bounded waits: its error flag stays clear
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.counter[1] = 0;
+    }
 
     for (int t = blockIdx.x; t < a.n_items; t += gridDim.x) {
         const int item = __ldg(a.queue + t);
@@ -89,10 +99,20 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
         // the item's step records (rate r), level plan and leaf codes (its 32 sites
         // of every leaf row), 16 bytes per thread and pass
         {
-            const int4* src = reinterpret_cast<const int4*>(a.recs + d.rec_off + size_t(r) * J * RB);
-            int4* dst = reinterpret_cast<int4*>(srec);
-            const int n = J * (RB / 16);
-            for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = __ldg(src + q);
+            if constexpr (FUSED) {
+                constexpr int R = rec_row_threads(KP);
+                const SchedNode* sc = a.sched + d.sched_off;
+                for (int q = threadIdx.x; q < J * 2 * R; q += blockDim.x) {
+                    const int s0 = q % R, c = (q / R) % 2, j = q / (2 * R);
+                    build_record_part<Real>(srec + size_t(j) * RB, sc[j], sc, d, a.params, a.blen, j,
+                                            a.K, KP, r, c, s0, R);
+                }
+            } else {
+                const int4* src = reinterpret_cast<const int4*>(a.recs + d.rec_off + size_t(r) * J * RB);
+                int4* dst = reinterpret_cast<int4*>(srec);
+                const int n = J * (RB / 16);
+                for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = __ldg(src + q);
+            }
             const int32_t* gplan = a.plan + d.plan_off;
             for (int q = threadIdx.x; q < 2 * J + 2; q += blockDim.x) splan[q] = __ldg(gplan + q);
             if (code_leaves) {
@@ -224,49 +244,113 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
         }
         __syncthreads();   // the next item restages the shared memory
     }
+    if constexpr (FUSED) {
+        // the last CTA to finish sums the partials of every item, in the order of the
+        // regular reduction (reduce_pass1/2, kernels_common.cu), so that one launch and
+        // three give the same bits: per split of the items, eight strided partial sums
+        // per branch added in order; for logL, 256 strided sums, a shuffle tree per
+        // 32 of them and the eight tree sums in order; then the splits in order
+        __shared__ int last;
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) last = atomicAdd(a.counter + 2, 1) == int(gridDim.x) - 1;
+        __syncthreads();
+        if (!last) return;
+        __threadfence();
+        const Real* pgrad = reinterpret_cast<const Real*>(a.pgrad);
+        for (int i = 0; i < a.n_inst; ++i) {
+            const InstanceDesc d = a.inst[i];
+            const int64_t n_items = int64_t(C) * d.n_blocks;
+            const int64_t per = (n_items + a.n_split - 1) / a.n_split;
+            if (w == 0) {
+                double tot = 0.0;
+                for (int z = 0; z < a.n_split; ++z) {
+                    const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
+                    double s = 0.0;
+                    for (int y = 0; y < RY; ++y) {
+                        double acc = 0.0;
+                        for (int64_t q = q0 + y * 32 + lane; q < q1; q += 32 * RY)
+                            acc += __ldcg(a.pll + d.item_off + q);
+                        s += warp_sum(acc);
+                    }
+                    tot += s;
+                }
+                if (lane == 0) a.out[i] = tot;
+            }
+            if (!a.want_grad) continue;
+            for (int b = threadIdx.x; b < d.n_branch; b += blockDim.x) {
+                const Real* pg = pgrad + d.pgrad_off + b;
+                double tot = 0.0;
+                for (int z = 0; z < a.n_split; ++z) {
+                    const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
+                    double s = 0.0;
+                    for (int y = 0; y < RY; ++y) {
+                        double acc = 0.0;
+                        for (int64_t q = q0 + y; q < q1; q += RY) acc += double(__ldcg(pg + q * d.n_branch));
+                        s += acc;
+                    }
+                    tot += s;
+                }
+                a.out[a.n_inst + d.grad_off + b] = tot;
+            }
+        }
+        if (threadIdx.x == 0) a.counter[2] = 0;   // ready for the next evaluation
+    }
 }
 
 // Dynamic shared memory allowed for each instantiation, per device: raised to the
 // largest size any layout asked for and never lowered (launch_attr.h).
-template <int KP, typename Real>
+template <int KP, typename Real, bool FUSED>
 static cudaError_t allow_smem(int smem) {
     static SmemAllowance allowance;
     return raise_smem(allowance, smem, [](int bytes) {
-        return cudaFuncSetAttribute(prune_level_kernel<KP, Real>,
+        return cudaFuncSetAttribute(prune_level_kernel<KP, Real, FUSED>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     });
 }
 
-template <int KP, typename Real>
+template <int KP, typename Real, bool FUSED>
 static cudaError_t go_level(int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
     const int smem = level_smem_bytes(KP, int(sizeof(Real)), a.max_J, tpb / 32);
-    cudaError_t e = allow_smem<KP, Real>(smem);
+    cudaError_t e = allow_smem<KP, Real, FUSED>(smem);
     if (e != cudaSuccess) return e;
-    prune_level_kernel<KP, Real><<<blocks, tpb, smem, st>>>(a);
+    prune_level_kernel<KP, Real, FUSED><<<blocks, tpb, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 template <int KP, typename Real>
 static cudaError_t occ_level(int tpb, int max_J, int* bps) {
     const int smem = level_smem_bytes(KP, int(sizeof(Real)), max_J, tpb / 32);
-    cudaError_t e = allow_smem<KP, Real>(smem);
+    cudaError_t e = allow_smem<KP, Real, false>(smem);
+    if (e == cudaSuccess) e = allow_smem<KP, Real, true>(smem);
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_level_kernel<KP, Real>, tpb, smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, prune_level_kernel<KP, Real, false>, tpb, smem);
 }
 
 bool level_supported(int kp) { return kp == 2 || kp == 4 || kp == 8; }
 
-cudaError_t launch_prune_level(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
-                               cudaStream_t st) {
+template <bool FUSED>
+static cudaError_t level_dispatch(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
+                                  cudaStream_t st) {
     switch (Kp * 2 + (f64 ? 1 : 0)) {
-        case 4: return go_level<2, float>(blocks, tpb, a, st);
-        case 5: return go_level<2, double>(blocks, tpb, a, st);
-        case 8: return go_level<4, float>(blocks, tpb, a, st);
-        case 9: return go_level<4, double>(blocks, tpb, a, st);
-        case 16: return go_level<8, float>(blocks, tpb, a, st);
-        case 17: return go_level<8, double>(blocks, tpb, a, st);
+        case 4: return go_level<2, float, FUSED>(blocks, tpb, a, st);
+        case 5: return go_level<2, double, FUSED>(blocks, tpb, a, st);
+        case 8: return go_level<4, float, FUSED>(blocks, tpb, a, st);
+        case 9: return go_level<4, double, FUSED>(blocks, tpb, a, st);
+        case 16: return go_level<8, float, FUSED>(blocks, tpb, a, st);
+        case 17: return go_level<8, double, FUSED>(blocks, tpb, a, st);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_prune_level(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
+                               cudaStream_t st) {
+    return level_dispatch<false>(f64, Kp, blocks, tpb, a, st);
+}
+
+cudaError_t launch_prune_level_fused(bool f64, int Kp, int blocks, int tpb, const PruneArgs& a,
+                                     cudaStream_t st) {
+    return level_dispatch<true>(f64, Kp, blocks, tpb, a, st);
 }
 
 cudaError_t occupancy_prune_level(bool f64, int Kp, int tpb, int max_J, int* bps) {

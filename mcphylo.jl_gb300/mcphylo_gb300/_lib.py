@@ -96,6 +96,34 @@ class NoDeviceError(MCPhyError):
     """No CUDA device: the engine has no CPU fallback."""
 
 
+class _Raw:
+    """Prototypes of the per-evaluation entry points that take addresses as plain
+    integers (no ctypes pointer objects to build per call), for hot loops."""
+
+    def __init__(self, L):
+        vp = ctypes.c_void_p
+
+        def proto(name, args):
+            f = L[name]            # a new function object: its own argtypes
+            f.restype = c_int
+            f.argtypes = args
+            return f
+
+        self.set_branch_lengths = proto("mcphy_set_branch_lengths", [vp, vp])
+        self.logpdf_grad = proto("mcphy_logpdf_grad", [vp, vp, vp])
+        self.logpdf = proto("mcphy_logpdf", [vp, vp])
+
+
+_raw = None
+
+
+def raw() -> _Raw:
+    global _raw
+    if _raw is None:
+        _raw = _Raw(load())
+    return _raw
+
+
 def load():
     """Load the shared library (raises if it has not been built)."""
     global _lib

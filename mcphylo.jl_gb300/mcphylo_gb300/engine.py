@@ -197,6 +197,50 @@ class Engine:
             return float(ll[0]), g
         return ll, g
 
+    def bind(self, i: int = 0):
+        """(grad_fn, logf_fn) for a sampler that evaluates this single-instance
+        handle thousands of times at new branch lengths: grad_fn(blen) -> (ll, grad)
+        and logf_fn(blen) -> ll.  The input and output buffers are allocated once and
+        their addresses passed as plain integers, so a call costs two C calls and a
+        copy of blen.  The returned grad array is reused by the next call (copy it to
+        keep it).  A new topology on the same nodes (set_tree with N nodes again) keeps
+        the binding valid; another node count needs a new bind()."""
+        if self.M != 1:
+            raise ValueError("bind() is for single-instance handles")
+        n = self._N[0] - 1
+        buf_b = np.empty(n, dtype=np.float64)
+        buf_ll = np.empty(1, dtype=np.float64)
+        buf_g = np.empty(n, dtype=np.float64)
+        pb, pll, pg = buf_b.ctypes.data, buf_ll.ctypes.data, buf_g.ctypes.data
+        raw = _lib.raw()
+        setb, lg, lf = raw.set_branch_lengths, raw.logpdf_grad, raw.logpdf
+        h = self._h.value
+
+        def fail(st, what):
+            check(st, self._h, what)
+
+        def grad_fn(blen):
+            np.copyto(buf_b, blen)
+            st = setb(h, pb)
+            if st:
+                fail(st, "set_branch_lengths")
+            st = lg(h, pll, pg)
+            if st:
+                fail(st, "logpdf_grad")
+            return float(buf_ll[0]), buf_g
+
+        def logf_fn(blen):
+            np.copyto(buf_b, blen)
+            st = setb(h, pb)
+            if st:
+                fail(st, "set_branch_lengths")
+            st = lf(h, pll)
+            if st:
+                fail(st, "logpdf")
+            return float(buf_ll[0])
+
+        return grad_fn, logf_fn
+
     def logpdf_grad_device(self, d_ll_ptr: int, d_grad_ptr: int) -> None:
         check(self._L.mcphy_logpdf_grad_device(self._h, ctypes.c_void_p(d_ll_ptr),
                                                ctypes.c_void_p(d_grad_ptr)), self._h)

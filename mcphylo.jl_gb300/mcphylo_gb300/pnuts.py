@@ -229,16 +229,25 @@ class TreePosterior:
         self._prop_parent: Optional[np.ndarray] = None
         engine.set_tree(self._parent, blen)
         self.n_set_tree = 0
+        # per engine: (grad_fn, logf_fn) bound to its handle (Engine.bind)
+        self._bound = {}
 
-    def _main(self, parent, blen):
+    def _fns(self, e):
+        f = self._bound.get(id(e))
+        if f is None:
+            f = self._bound[id(e)] = e.bind()
+        return f
+
+    def _main(self, parent):
+        """The engine holding `parent`, its topology updated when needed (the branch
+        lengths are sent by the evaluation itself)."""
         if np.array_equal(parent, self._parent):
-            self.eng.set_branch_lengths(blen)
+            pass
         elif self._prop_parent is not None and np.array_equal(parent, self._prop_parent):
             self.eng, self.prop = self.prop, self.eng
             self._parent, self._prop_parent = self._prop_parent, self._parent
-            self.eng.set_branch_lengths(blen)
         else:
-            self.eng.set_tree(parent, blen)
+            self.eng.set_tree(parent)
             self._parent = np.asarray(parent, dtype=np.int64).copy()
             self.n_set_tree += 1
         return self.eng
@@ -249,21 +258,19 @@ class TreePosterior:
         return self.prior.logpdf_grad(parent, blen)
 
     def logfgrad(self, parent, blen):
-        ll, g = self._main(parent, blen).logpdf_grad()
+        ll, g = self._fns(self._main(parent))[0](blen)
         lp, gp = self._prior(parent, blen)
         return ll + lp, g + gp
 
     def logf(self, parent, blen):
         if self.prop is not None and not np.array_equal(parent, self._parent):
-            if self._prop_parent is not None and np.array_equal(parent, self._prop_parent):
-                self.prop.set_branch_lengths(blen)
-            else:
-                self.prop.set_tree(parent, blen)
+            if self._prop_parent is None or not np.array_equal(parent, self._prop_parent):
+                self.prop.set_tree(parent)
                 self._prop_parent = np.asarray(parent, dtype=np.int64).copy()
                 self.n_set_tree += 1
-            ll = self.prop.logpdf()
+            ll = self._fns(self.prop)[1](blen)
         else:
-            ll = self._main(parent, blen).logpdf()
+            ll = self._fns(self._main(parent))[1](blen)
         return ll + self._prior(parent, blen)[0]
 
 

@@ -250,20 +250,25 @@ def test_dual_averaging_moves_step_size():
 
 
 class _FakeEngine:
+    """Records the calls a TreePosterior makes: topology updates and evaluations
+    (each bound evaluation sends its branch lengths)."""
+
     def __init__(self, tag, log):
         self.tag, self.log = tag, log
 
-    def set_tree(self, parent, blen):
+    def set_tree(self, parent, blen=None):
         self.log.append((self.tag, "tree", tuple(parent)))
 
-    def set_branch_lengths(self, blen):
-        self.log.append((self.tag, "blen"))
+    def bind(self):
+        def grad_fn(blen):
+            self.log.append((self.tag, "blen"))
+            return -1.0, np.zeros(6)
 
-    def logpdf(self):
-        return -1.0
+        def logf_fn(blen):
+            self.log.append((self.tag, "blen"))
+            return -1.0
 
-    def logpdf_grad(self):
-        return -1.0, np.zeros(6)
+        return grad_fn, logf_fn
 
 
 def test_tree_posterior_routes_proposals():
@@ -275,7 +280,7 @@ def test_tree_posterior_routes_proposals():
     post.logfgrad(PARENT_A, np.ones(6))
     post.logf(PARENT_B, np.ones(6))            # proposal goes to b
     post.logf(PARENT_A, np.ones(6))            # rejected: a still holds A
-    assert log == [("a", "blen"), ("b", "tree", tuple(PARENT_B)), ("a", "blen")]
+    assert log == [("a", "blen"), ("b", "tree", tuple(PARENT_B)), ("b", "blen"), ("a", "blen")]
     log.clear()
     post.logf(PARENT_B, np.ones(6))            # proposed again: b already holds B
     post.logfgrad(PARENT_B, np.ones(6))        # accepted: the engines trade places
