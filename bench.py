@@ -89,15 +89,16 @@ def make_engine(insts, precision, tiles=None, sweep="auto"):
     return e
 
 
-def tc_algorithmic_bytes(insts, grad=True, bf16=False):
+def tc_algorithmic_bytes(insts, grad=True, prec="tf32"):
     """Bytes the tensor-core kernel must move per evaluation: every post-order partial
     of an internal non-root step written once (as an operand tile, KD entries per
-    site, 4 bytes in TF32 and 2 in BF16) and read once by the gradient sweep, the leaf
-    state codes read once (4 bytes), the per-item gradient partials written once."""
+    site, 4 bytes in TF32, 2 in BF16, 8 in split TF32: value and residual) and read
+    once by the gradient sweep, the leaf state codes read once (4 bytes), the per-item
+    gradient partials written once."""
     import mcphylo_gb300 as mp
     total = 0
-    step = 16 if bf16 else 8
-    esz = 2 if bf16 else 4
+    step = 16 if prec == "bf16" else 8
+    esz = {"bf16": 2, "tf32": 4, "tf32x3": 8}[prec]
     for b in insts:
         KD = (b.K + step - 1) // step * step
         info = mp.schedule_info(b.parent)
@@ -456,9 +457,9 @@ def run_gpu(args, rank, world):
     peak_kind = "measured" if "hbm_gbs" in peaks else "fallback"
 
     prec = args.precision
-    tc_path = prec in ("tf32", "bf16")
+    tc_path = prec in ("tf32", "bf16", "tf32x3")
     if tc_path and insts[0].K < 9:
-        raise SystemExit("--precision tf32/bf16 is the dense-state path (K >= 9)")
+        raise SystemExit("--precision tf32/bf16/tf32x3 is the dense-state path (K >= 9)")
     if args.tiles == "auto" and args.sweep == "auto":
         # the library's autotuner: times each sweep and launch shape on this problem
         e = make_engine(insts, prec)
@@ -642,7 +643,7 @@ def run_gpu(args, rank, world):
     K0 = insts[0].K
     kp = 2 if K0 <= 2 else 4 if K0 <= 4 else 8 if K0 <= 8 else 20 if K0 <= 20 else 32
     if tc_path:
-        alg = tc_algorithmic_bytes(insts, args.mode == "grad", prec == "bf16")
+        alg = tc_algorithmic_bytes(insts, args.mode == "grad", prec)
         kname = "prune_tc_kernel<%d,%s>" % ((K0 + 7) // 8 * 8, prec)
     elif sweep == "level":
         alg = level_algorithmic_bytes(insts, real_b, args.mode == "grad")
@@ -735,9 +736,9 @@ def main():
     ap.add_argument("--nuts-adapt", type=int, default=200)
     ap.add_argument("--nuts-seed", type=int, default=1)
     ap.add_argument("--nuts-target", type=float, default=0.8)
-    ap.add_argument("--precision", default="f32", choices=["f32", "tf32", "bf16"],
-                    help="f32: FP32-scaled SIMT path; tf32 / bf16: tensor-core node updates "
-                         "with TF32 / BF16 operands (K >= 9)")
+    ap.add_argument("--precision", default="f32", choices=["f32", "tf32", "bf16", "tf32x3"],
+                    help="f32: FP32-scaled SIMT path; tf32 / bf16 / tf32x3: tensor-core node "
+                         "updates with TF32 / BF16 / split-TF32 operands (K >= 9)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

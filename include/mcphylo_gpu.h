@@ -57,7 +57,11 @@ typedef enum {
     MCPHY_PREC_TF32 = 2,      /* K >= 9 only: node updates as TF32 tensor-core products
                                  (tcgen05, FP32 accumulation), the rest as MCPHY_PREC_F32;
                                  state-code leaves only                                  */
-    MCPHY_PREC_BF16 = 3       /* as MCPHY_PREC_TF32 with BF16 operands                   */
+    MCPHY_PREC_BF16 = 3,      /* as MCPHY_PREC_TF32 with BF16 operands                   */
+    MCPHY_PREC_TF32X3 = 4     /* 9 <= K <= 24: as MCPHY_PREC_TF32 with every operand split
+                                 into a TF32 value and a TF32 residual, each product the
+                                 three MMAs lo*hi + hi*lo + hi*hi: about 21 bits per
+                                 operand, FP32-level accuracy on the tensor cores        */
 } mcphy_precision;
 
 /* ------------------------------------------------------------------ single tree

@@ -126,7 +126,10 @@ int check_instance(mcphy_engine* h, int64_t i) {
 size_t real_size(const mcphy_engine* h) { return h->prec == MCPHY_PREC_F64 ? 8 : 4; }
 // tensor-core path: -1 none, 0 TF32 operands, 1 BF16 operands
 int tc_fmt(const mcphy_engine* h) {
-    return h->prec == MCPHY_PREC_TF32 ? 0 : h->prec == MCPHY_PREC_BF16 ? 1 : -1;
+    return h->prec == MCPHY_PREC_TF32    ? 0
+           : h->prec == MCPHY_PREC_BF16  ? 1
+           : h->prec == MCPHY_PREC_TF32X3 ? 2
+                                         : -1;
 }
 
 // Level-synchronous sweep: supported state spaces, and whether a CTA's shared
@@ -891,11 +894,15 @@ int mcphy_batch_create(int64_t nbase, int64_t nrates, int64_t n_instances, int p
     if (nrates < 1 || nrates > 64) return MCPHY_ERR_ARG;
     if (n_instances < 1 || n_instances > 65535) return MCPHY_ERR_ARG;
     if (precision != MCPHY_PREC_F32 && precision != MCPHY_PREC_F64 &&
-        precision != MCPHY_PREC_TF32 && precision != MCPHY_PREC_BF16)
+        precision != MCPHY_PREC_TF32 && precision != MCPHY_PREC_BF16 &&
+        precision != MCPHY_PREC_TF32X3)
         return MCPHY_ERR_ARG;
-    // the tensor-core node updates are for dense state spaces (K >= 9)
-    if ((precision == MCPHY_PREC_TF32 || precision == MCPHY_PREC_BF16) && nbase < 9)
+    // the tensor-core node updates are for dense state spaces (K >= 9); the split
+    // operands of K > 24 do not fit one CTA's shared memory
+    if ((precision == MCPHY_PREC_TF32 || precision == MCPHY_PREC_BF16 ||
+         precision == MCPHY_PREC_TF32X3) && nbase < 9)
         return MCPHY_ERR_ARG;
+    if (precision == MCPHY_PREC_TF32X3 && nbase > 24) return MCPHY_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();

@@ -141,16 +141,25 @@ struct PruneArgs {
 constexpr int TC_M = 128;
 constexpr int TC_N = 32;
 constexpr int TC_HDR = 64;
-// operand format: 0 = TF32 (4-byte elements, 8 per MMA K step), 1 = BF16 (2-byte, 16)
-__host__ __device__ constexpr int tc_esz(int fmt) { return fmt ? 2 : 4; }
-__host__ __device__ constexpr int tc_kstep(int fmt) { return fmt ? 16 : 8; }
+// operand format: 0 = TF32 (4-byte elements, 8 per MMA K step), 1 = BF16 (2-byte, 16),
+// 2 = split TF32 ("3xTF32"): every operand tile is a TF32 tile of the value rounded
+// (hi) followed by a TF32 tile of the rounding residual (lo), and a product is the
+// three MMAs A_lo B_hi + A_hi B_lo + A_hi B_hi accumulated in FP32 -- about 21
+// mantissa bits per operand instead of 10
+__host__ __device__ constexpr int tc_esz(int fmt) { return fmt == 1 ? 2 : 4; }
+__host__ __device__ constexpr int tc_kstep(int fmt) { return fmt == 1 ? 16 : 8; }
+__host__ __device__ constexpr int tc_split(int fmt) { return fmt == 2 ? 2 : 1; }   // tiles per operand
 __host__ __device__ constexpr int tc_vk(int K) { return (K + 7) / 8 * 8; }   // register vectors
 __host__ __device__ constexpr int tc_kd(int K, int fmt) {                     // operand K extent
     return (K + tc_kstep(fmt) - 1) / tc_kstep(fmt) * tc_kstep(fmt);
 }
 __host__ __device__ constexpr int tc_k4(int K) { return (K + 3) / 4 * 4; }
-__host__ __device__ constexpr int tc_atile(int K, int fmt) { return TC_M * tc_kd(K, fmt) * tc_esz(fmt); }
-__host__ __device__ constexpr int tc_tile(int K, int fmt) { return TC_N * tc_kd(K, fmt) * tc_esz(fmt); }
+// bytes of one operand (both parts for the split format); the lo part of a split
+// operand starts tc_half_* bytes after its hi part
+__host__ __device__ constexpr int tc_half_atile(int K, int fmt) { return TC_M * tc_kd(K, fmt) * tc_esz(fmt); }
+__host__ __device__ constexpr int tc_half_tile(int K, int fmt) { return TC_N * tc_kd(K, fmt) * tc_esz(fmt); }
+__host__ __device__ constexpr int tc_atile(int K, int fmt) { return tc_split(fmt) * tc_half_atile(K, fmt); }
+__host__ __device__ constexpr int tc_tile(int K, int fmt) { return tc_split(fmt) * tc_half_tile(K, fmt); }
 __host__ __device__ constexpr int tc_tab(int K) { return K * tc_k4(K) * 4; }
 __host__ __device__ constexpr int tc_rs(int K) { return tc_k4(K) * 4; }
 __host__ __device__ constexpr int tc_fchild(int K, int fmt) { return tc_tile(K, fmt) + tc_tab(K) + tc_rs(K); }
@@ -1142,7 +1151,7 @@ struct GatherArgs {
 cudaError_t launch_gather_codes(const GatherArgs& a, cudaStream_t st);
 
 // Tensor-core path (kernels_tc.cu).
-// fmt: 0 = TF32, 1 = BF16 operands
+// fmt: 0 = TF32, 1 = BF16, 2 = split TF32 operands
 cudaError_t launch_build_records_tc(int fmt, const BuildRecArgs& a, cudaStream_t st);
 cudaError_t launch_prune_tc(int fmt, int K, int blocks, const PruneArgs& a, cudaStream_t st);
 cudaError_t occupancy_prune_tc(int fmt, int K, int* blocks_per_sm);

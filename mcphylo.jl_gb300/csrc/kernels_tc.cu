@@ -108,11 +108,18 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
     float* drs = reinterpret_cast<float*>(bk + 2 * TB + tc_tab(K));
     // operand-tile element (row, col) in the tile format (TF32-rounded or BF16)
     auto put = [&](unsigned char* tile, int row, int col, float v) {
-        if constexpr (FMT == 0)
+        if constexpr (FMT == 0) {
             *reinterpret_cast<float*>(tile + tc::tile_off_e<4>(row, col, KD)) = tc::to_tf32(v);
-        else
+        } else if constexpr (FMT == 2) {
+            // hi: v rounded to TF32; lo (the next tile): the residual rounded to TF32
+            const float hi = tc::to_tf32(v);
+            *reinterpret_cast<float*>(tile + tc::tile_off_e<4>(row, col, KD)) = hi;
+            *reinterpret_cast<float*>(tile + tc_half_tile(K, FMT) + tc::tile_off_e<4>(row, col, KD)) =
+                tc::to_tf32(v - hi);
+        } else {
             *reinterpret_cast<__nv_bfloat16*>(tile + tc::tile_off_e<2>(row, col, KD)) =
                 __float2bfloat16_rn(v);
+        }
     };
     const int b = sn.br[c];
     const bool real = b < d.n_branch;
@@ -251,6 +258,21 @@ __device__ __forceinline__ void write_a(unsigned char* tile, int row, const floa
             *reinterpret_cast<float4*>(tile + tc::tile_off_e<4>(row, k, VK)) =
                 make_float4(tc::to_tf32(v[k]), tc::to_tf32(v[k + 1]), tc::to_tf32(v[k + 2]),
                             tc::to_tf32(v[k + 3]));
+    } else if constexpr (FMT == 2) {
+        // the hi tile, then the lo tile (residuals) TC_M x VK x 4 bytes after it
+#pragma unroll
+        for (int k = 0; k < VK; k += 4) {
+            float hi[4], lo[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                hi[q] = tc::to_tf32(v[k + q]);
+                lo[q] = tc::to_tf32(v[k + q] - hi[q]);
+            }
+            *reinterpret_cast<float4*>(tile + tc::tile_off_e<4>(row, k, VK)) =
+                make_float4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<float4*>(tile + TC_M * VK * 4 + tc::tile_off_e<4>(row, k, VK)) =
+                make_float4(lo[0], lo[1], lo[2], lo[3]);
+        }
     } else {
         constexpr int KD = (VK + 15) / 16 * 16;
 #pragma unroll
@@ -301,10 +323,11 @@ __device__ __forceinline__ void col_store(float* col, int slot, int K, int t, co
 // ahead from the lookahead fields of the step record headers.
 template <int VK, int FMT>
 __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
-    constexpr int ESZ = FMT ? 2 : 4;                  // operand element bytes
-    constexpr int KSTEP = FMT ? 16 : 8;               // K of one MMA instruction
+    constexpr int ESZ = FMT == 1 ? 2 : 4;             // operand element bytes
+    constexpr int KSTEP = FMT == 1 ? 16 : 8;          // K of one MMA instruction
     constexpr int KD = (VK + KSTEP - 1) / KSTEP * KSTEP;   // operand K extent
-    constexpr int TILE = TC_M * KD * ESZ;             // bytes of one A tile
+    constexpr int AHALF = TC_M * KD * ESZ;            // bytes of one A tile part
+    constexpr int TILE = tc_split(FMT) * AHALF;       // bytes of one A operand
     extern __shared__ __align__(1024) unsigned char sm[];
     const int K = a.K, K4 = tc_k4(a.K), C = a.C;
     const int RB = tc_rec_bytes(K, FMT), FB = tc_fwd_bytes(K, FMT);
@@ -332,7 +355,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
     tc::fence_after_sync();
     const uint32_t tbase = *tslot;
     const uint32_t tl = tbase + (uint32_t(warp * 32) << 16);     // this warp's lane quarter
-    const uint32_t idesc = FMT ? tc::idesc_bf16(TC_M, TC_N) : tc::idesc_tf32(TC_M, TC_N);
+    const uint32_t idesc = FMT == 1 ? tc::idesc_bf16(TC_M, TC_N) : tc::idesc_tf32(TC_M, TC_N);
     const uint32_t sbo = uint32_t(tc::tile_sbo_e<ESZ>(KD));
     unsigned char* post = reinterpret_cast<unsigned char*>(a.post) +
                           size_t(blockIdx.x) * size_t(a.warp_stride) * 4;
@@ -381,12 +404,26 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
         if (t == 0) {
             for (int i = 0; i < n; ++i) {
                 const uint32_t a0 = tc::smem_addr(at[i]), b0 = tc::smem_addr(bt[i]);
+                if constexpr (FMT == 2) {
+                    // A_lo B_hi + A_hi B_lo + A_hi B_hi, the small terms first
+                    constexpr uint32_t BHALF = TC_N * KD * 4;
+                    const uint32_t pa[3] = {a0 + AHALF, a0, a0}, pb[3] = {b0, b0 + BHALF, b0};
 #pragma unroll
-                for (int s = 0; s < KD / KSTEP; ++s) {
-                    const uint64_t ad = tc::smem_desc(a0 + 256u * s, tc::kCoreBytes, sbo);
-                    const uint64_t bd = tc::smem_desc(b0 + 256u * s, tc::kCoreBytes, sbo);
-                    if constexpr (FMT == 0) tc::mma_tf32(tbase + dcol[i], ad, bd, idesc, s > 0 ? 1u : 0u);
-                    else tc::mma_bf16(tbase + dcol[i], ad, bd, idesc, s > 0 ? 1u : 0u);
+                    for (int p = 0; p < 3; ++p)
+#pragma unroll
+                        for (int s = 0; s < KD / KSTEP; ++s) {
+                            const uint64_t ad = tc::smem_desc(pa[p] + 256u * s, tc::kCoreBytes, sbo);
+                            const uint64_t bd = tc::smem_desc(pb[p] + 256u * s, tc::kCoreBytes, sbo);
+                            tc::mma_tf32(tbase + dcol[i], ad, bd, idesc, (p > 0 || s > 0) ? 1u : 0u);
+                        }
+                } else {
+#pragma unroll
+                    for (int s = 0; s < KD / KSTEP; ++s) {
+                        const uint64_t ad = tc::smem_desc(a0 + 256u * s, tc::kCoreBytes, sbo);
+                        const uint64_t bd = tc::smem_desc(b0 + 256u * s, tc::kCoreBytes, sbo);
+                        if constexpr (FMT == 0) tc::mma_tf32(tbase + dcol[i], ad, bd, idesc, s > 0 ? 1u : 0u);
+                        else tc::mma_bf16(tbase + dcol[i], ad, bd, idesc, s > 0 ? 1u : 0u);
+                    }
                 }
             }
             tc::mma_commit(bars + 2);
@@ -750,31 +787,38 @@ cudaError_t launch_build_records_tc(int fmt, const BuildRecArgs& a, cudaStream_t
     const int64_t total = std::max<int64_t>(1, int64_t(a.n_steps) * 2 * a.C * TC_N);
     const int tpb = 128;
     const unsigned blocks = unsigned((total + tpb - 1) / tpb);
-    if (fmt) build_records_tc_kernel<1><<<blocks, tpb, 0, st>>>(a);
+    if (fmt == 1) build_records_tc_kernel<1><<<blocks, tpb, 0, st>>>(a);
+    else if (fmt == 2) build_records_tc_kernel<2><<<blocks, tpb, 0, st>>>(a);
     else build_records_tc_kernel<0><<<blocks, tpb, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_prune_tc(int fmt, int K, int blocks, const PruneArgs& a, cudaStream_t st) {
-    switch (tc_vk(K) * 2 + (fmt ? 1 : 0)) {
-        case 32: return go_tc<16, 0>(blocks, a, st);
-        case 33: return go_tc<16, 1>(blocks, a, st);
-        case 48: return go_tc<24, 0>(blocks, a, st);
-        case 49: return go_tc<24, 1>(blocks, a, st);
-        case 64: return go_tc<32, 0>(blocks, a, st);
-        case 65: return go_tc<32, 1>(blocks, a, st);
+    switch (tc_vk(K) * 3 + fmt) {
+        case 48: return go_tc<16, 0>(blocks, a, st);
+        case 49: return go_tc<16, 1>(blocks, a, st);
+        case 50: return go_tc<16, 2>(blocks, a, st);
+        case 72: return go_tc<24, 0>(blocks, a, st);
+        case 73: return go_tc<24, 1>(blocks, a, st);
+        case 74: return go_tc<24, 2>(blocks, a, st);
+        case 96: return go_tc<32, 0>(blocks, a, st);
+        case 97: return go_tc<32, 1>(blocks, a, st);
+        case 98: return go_tc<32, 2>(blocks, a, st);
         default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t occupancy_prune_tc(int fmt, int K, int* bps) {
-    switch (tc_vk(K) * 2 + (fmt ? 1 : 0)) {
-        case 32: return occ_tc<16, 0>(K, bps);
-        case 33: return occ_tc<16, 1>(K, bps);
-        case 48: return occ_tc<24, 0>(K, bps);
-        case 49: return occ_tc<24, 1>(K, bps);
-        case 64: return occ_tc<32, 0>(K, bps);
-        case 65: return occ_tc<32, 1>(K, bps);
+    switch (tc_vk(K) * 3 + fmt) {
+        case 48: return occ_tc<16, 0>(K, bps);
+        case 49: return occ_tc<16, 1>(K, bps);
+        case 50: return occ_tc<16, 2>(K, bps);
+        case 72: return occ_tc<24, 0>(K, bps);
+        case 73: return occ_tc<24, 1>(K, bps);
+        case 74: return occ_tc<24, 2>(K, bps);
+        case 96: return occ_tc<32, 0>(K, bps);
+        case 97: return occ_tc<32, 1>(K, bps);
+        case 98: return occ_tc<32, 2>(K, bps);
         default: return cudaErrorInvalidValue;
     }
 }

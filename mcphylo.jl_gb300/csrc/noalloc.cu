@@ -160,7 +160,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
         h->err = "no evaluation has run on this handle yet";
         return MCPHY_ERR_STATE;
     }
-    if (h->prec == MCPHY_PREC_TF32 || h->prec == MCPHY_PREC_BF16) {
+    if (h->prec == MCPHY_PREC_TF32 || h->prec == MCPHY_PREC_BF16 || h->prec == MCPHY_PREC_TF32X3) {
         h->err = "the allocation-free entry point runs the FP32 and FP64 kernels only";
         return MCPHY_ERR_ARG;
     }

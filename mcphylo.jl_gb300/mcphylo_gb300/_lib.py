@@ -20,6 +20,7 @@ PREC_F32 = 0
 PREC_F64 = 1
 PREC_TF32 = 2
 PREC_BF16 = 3
+PREC_TF32X3 = 4
 
 i64 = ctypes.c_int64
 c_int = ctypes.c_int

@@ -17,7 +17,7 @@ from ._lib import check
 
 _PREC = {"f32": _lib.PREC_F32, "fp32": _lib.PREC_F32, "float32": _lib.PREC_F32,
          "f64": _lib.PREC_F64, "fp64": _lib.PREC_F64, "float64": _lib.PREC_F64,
-         "tf32": _lib.PREC_TF32, "bf16": _lib.PREC_BF16}
+         "tf32": _lib.PREC_TF32, "bf16": _lib.PREC_BF16, "tf32x3": _lib.PREC_TF32X3}
 
 
 def _pd(a: np.ndarray):

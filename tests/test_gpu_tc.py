@@ -202,3 +202,41 @@ def test_bf16_vs_oracle(built_lib, K, C, taxa, S, mf):
     assert rel <= BF16_LL_RTOL
     assert gerr <= BF16_G_RTOL
     assert e.logpdf() == pytest.approx(ll, rel=1e-12)
+
+
+# ---------------------------------------------------------------- split TF32 (3xTF32)
+# Every operand is a TF32 value plus a TF32 residual and each product is three MMAs
+# (lo*hi + hi*lo + hi*hi), about 21 bits per operand: held to the FP32 path's own
+# tolerances against the FP64 oracle (logL 1e-6 relative; gradient entries 1e-4
+# relative to max(|g_i|, 1e-2 max|g|)).
+@pytest.mark.parametrize("K,C,taxa,S,mf", [(20, 4, 24, 300, 0.0), (20, 1, 40, 128, 0.3),
+                                         (9, 2, 17, 77, 0.0), (12, 3, 30, 257, 0.2),
+                                         (24, 2, 12, 140, 0.0)])
+def test_tf32x3_vs_oracle(built_lib, K, C, taxa, S, mf):
+    from gpu_cases import F32_G_FLOOR, F32_G_RTOL, F32_LL_RTOL, assert_grad_close
+    inst = random_instance(K, C, taxa, S, seed=K * 13 + taxa, multifurcate=mf)
+    llo, go = oracle(inst)
+    e = _tf32_engine(inst, "tf32x3")
+    ll, g = e.logpdf_grad()
+    rel = abs(ll - llo) / abs(llo)
+    gerr = assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
+    print(f"tf32x3 K={K} N={inst.N} S={S}: logL rel {rel:.2e}, grad {gerr:.2e}")
+    assert rel <= F32_LL_RTOL, (ll, llo)
+    assert e.logpdf() == pytest.approx(ll, rel=1e-12)
+
+
+def test_tf32x3_deep_caterpillar(built_lib):
+    from gpu_cases import F32_G_FLOOR, F32_G_RTOL, F32_LL_RTOL, assert_grad_close
+    rng = np.random.default_rng(3)
+    inst = random_instance(20, 2, 0, 200, seed=3, tree=caterpillar(60, rng))
+    llo, go = oracle(inst)
+    ll, g = _tf32_engine(inst, "tf32x3").logpdf_grad()
+    assert abs(ll - llo) <= F32_LL_RTOL * abs(llo), (ll, llo)
+    assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
+
+
+def test_tf32x3_rejects_unsupported_state_spaces(built_lib):
+    import mcphylo_gb300 as mp
+    for K in (4, 25, 32):
+        with pytest.raises(Exception):
+            mp.Engine(K, 2, "tf32x3")
