@@ -1047,12 +1047,17 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
     const double mu = Uinv[K * K];
     const double rate = Uinv[K * K + 1 + r];
     const double t = blen[d.blen_off + b];
-    double e[32], de[32];
+    // P = U diag(exp(x)) Uinv written as I + U diag(expm1(x)) Uinv: the same matrix,
+    // without the cancellation of O(1) terms that leaves the reference's formula
+    // (parallel_transition_prob, VectorizedFunctions.jl:155-168) with a relative error
+    // of up to ~1e-9 in the off-diagonal entries of short branches (t ~ 1e-5);
+    // dP/dt = U diag(D r mu exp(x)) Uinv as the reference forms it
+    double em[32], de[32];
     if (s0 < K)
         for (int m = 0; m < K; ++m) {
-            const double x = exp(mu * t * Dv[m] * rate);
-            e[m] = x;
-            de[m] = Dv[m] * rate * mu * x;
+            const double x = mu * t * Dv[m] * rate;
+            em[m] = expm1(x);
+            de[m] = Dv[m] * rate * mu * exp(x);
         }
     for (int s = s0; s < Kp; s += R) {
         double rs = 0.0, drs = 0.0;
@@ -1060,9 +1065,10 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
             double p = 0.0, dp = 0.0;
             if (s < K && k < K) {
                 for (int m = 0; m < K; ++m) {
-                    p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                    p += U[s + K * m] * em[m] * Uinv[m + K * k];
                     dp += U[s + K * m] * de[m] * Uinv[m + K * k];
                 }
+                if (s == k) p += 1.0;
                 rs += p;
                 drs += dp;
             } else {

@@ -257,41 +257,60 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
         __syncthreads();
         if (!last) return;
         __threadfence();
+        // the shared memory of the sweep is free again: red[RY][CB] partial sums
+        double* red = reinterpret_cast<double*>(smem);
+        const int CB = int(blockDim.x) / RY;   // branches per pass, RY threads each
         const Real* pgrad = reinterpret_cast<const Real*>(a.pgrad);
         for (int i = 0; i < a.n_inst; ++i) {
             const InstanceDesc d = a.inst[i];
             const int64_t n_items = int64_t(C) * d.n_blocks;
             const int64_t per = (n_items + a.n_split - 1) / a.n_split;
-            if (w == 0) {
-                double tot = 0.0;
-                for (int z = 0; z < a.n_split; ++z) {
-                    const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
-                    double s = 0.0;
-                    for (int y = 0; y < RY; ++y) {
-                        double acc = 0.0;
-                        for (int64_t q = q0 + y * 32 + lane; q < q1; q += 32 * RY)
-                            acc += __ldcg(a.pll + d.item_off + q);
-                        s += warp_sum(acc);
-                    }
-                    tot += s;
+            // logL: 256 strided sums per split (warp w takes strided groups w, w + W, ..)
+            double tot = 0.0;
+            for (int z = 0; z < a.n_split; ++z) {
+                const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
+                for (int y = w; y < RY; y += W) {
+                    double acc = 0.0;
+                    for (int64_t q = q0 + y * 32 + lane; q < q1; q += 32 * RY)
+                        acc += __ldcg(a.pll + d.item_off + q);
+                    acc = warp_sum(acc);
+                    if (lane == 0) red[y] = acc;
                 }
-                if (lane == 0) a.out[i] = tot;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double s2 = 0.0;
+                    for (int y = 0; y < RY; ++y) s2 += red[y];
+                    tot += s2;
+                }
+                __syncthreads();
             }
+            if (threadIdx.x == 0) a.out[i] = tot;
             if (!a.want_grad) continue;
-            for (int b = threadIdx.x; b < d.n_branch; b += blockDim.x) {
-                const Real* pg = pgrad + d.pgrad_off + b;
-                double tot = 0.0;
+            // gradients: thread (bi, y) of a pass sums items y, y + RY, .. of its split
+            // for branch b0 + bi; thread bi then adds the RY sums in order
+            const int bi = int(threadIdx.x) / RY, y = int(threadIdx.x) % RY;
+            for (int b0 = 0; b0 < d.n_branch; b0 += CB) {
+                const int b = b0 + bi;
+                double gtot = 0.0;
                 for (int z = 0; z < a.n_split; ++z) {
                     const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
-                    double s = 0.0;
-                    for (int y = 0; y < RY; ++y) {
+                    if (bi < CB && b < d.n_branch) {
+                        const Real* pg = pgrad + d.pgrad_off + b;
                         double acc = 0.0;
+#pragma unroll 4
                         for (int64_t q = q0 + y; q < q1; q += RY) acc += double(__ldcg(pg + q * d.n_branch));
-                        s += acc;
+                        red[y * CB + bi] = acc;
                     }
-                    tot += s;
+                    __syncthreads();
+                    if (int(threadIdx.x) < CB && b0 + int(threadIdx.x) < d.n_branch) {
+                        double s2 = 0.0;
+                        for (int yy = 0; yy < RY; ++yy) s2 += red[yy * CB + threadIdx.x];
+                        gtot += s2;
+                    }
+                    __syncthreads();
                 }
-                a.out[a.n_inst + d.grad_off + b] = tot;
+                if (int(threadIdx.x) < CB && b0 + int(threadIdx.x) < d.n_branch)
+                    a.out[a.n_inst + d.grad_off + b0 + threadIdx.x] = gtot;
             }
         }
         if (threadIdx.x == 0) a.counter[2] = 0;   // ready for the next evaluation

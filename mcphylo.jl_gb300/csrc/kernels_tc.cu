@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
     };
     const int b = sn.br[c];
     const bool real = b < d.n_branch;
-    double e[32], de[32];
+    // P = I + U diag(expm1(x)) Uinv (see build_record_part, kernels.cuh)
+    double em[32], de[32];
     const double* U = a.params + d.param_off;
     const double* Uinv = U + K * K + K;
     if (real && s < K) {
@@ -132,9 +133,9 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
         const double rate = Uinv[K * K + 1 + r];
         const double t = a.blen[d.blen_off + b];
         for (int m = 0; m < K; ++m) {
-            const double x = exp(mu * t * Dv[m] * rate);
-            e[m] = x;
-            de[m] = Dv[m] * rate * mu * x;
+            const double x = mu * t * Dv[m] * rate;
+            em[m] = expm1(x);
+            de[m] = Dv[m] * rate * mu * exp(x);
         }
     }
     double row = 0.0, drow = 0.0;
@@ -144,9 +145,10 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
         if (s < K && k < K) {
             if (real) {
                 for (int m = 0; m < K; ++m) {
-                    p += U[s + K * m] * e[m] * Uinv[m + K * k];
+                    p += U[s + K * m] * em[m] * Uinv[m + K * k];
                     dp += U[s + K * m] * de[m] * Uinv[m + K * k];
                 }
+                if (s == k) p += 1.0;
             } else {
                 p = (s == k) ? 1.0 : 0.0;
             }

@@ -14,7 +14,12 @@ of a batch):
      its first <= 2,000 sites, all in one batched launch)
   5. 20-state GTR+G4, 256 taxa x 50,000 sites                     (500-site window)
 
-Bounds: FP64 logL 1e-12 relative, gradient 1e-10 of max|g| (per instance); FP32
+Bounds: FP64 logL 1e-12 relative, gradient 1e-10 of max|g| (per instance; 1e-9 on
+configuration 4, whose shortest branches, t ~ 1e-5, leave the reference's P(t) =
+U diag(exp) U^-1 -- followed by the oracle -- with relative errors up to ~6e-9 in its
+off-diagonal entries: the oracle is 1.2e-10 of max|g| from an extended-precision
+evaluation on one of its instances, while the engine builds P(t) as
+I + U diag(expm1) U^-1 without that cancellation); FP32
 logL 1e-6 relative, gradient entries 1e-4 relative to max(|g_i|, 1e-2 max|g|), and
 1e-4 relative with no floor on every entry whose condition number is at most 1000.
 The condition number of entry i is sum_{site,rate} |term| / |g_i| (from the
@@ -83,7 +88,7 @@ def engine_for(insts, precision, weights=None):
     return e
 
 
-def check(name, precision, ll, g, refs, off):
+def check(name, precision, ll, g, refs, off, f64_g_rtol=F64_G_RTOL):
     """refs: one (ll, grad, scale) of the oracle per instance; off: packed offsets."""
     ll = np.atleast_1d(ll)
     llo = np.array([r[0] for r in refs])
@@ -94,7 +99,7 @@ def check(name, precision, ll, g, refs, off):
     for i, r in enumerate(refs):   # the norm-wise / floored bounds use each instance's max|g|
         sl = slice(off[i], off[i + 1])
         if precision == "f64":
-            floored = max(floored, assert_grad_close(g[sl], r[1], F64_G_RTOL, F64_G_FLOOR))
+            floored = max(floored, assert_grad_close(g[sl], r[1], f64_g_rtol, F64_G_FLOOR))
         else:
             floored = max(floored, assert_grad_close(g[sl], r[1], F32_G_RTOL, F32_G_FLOOR))
     kappa = a / np.maximum(np.abs(go), 1e-300)
@@ -111,12 +116,12 @@ def check(name, precision, ll, g, refs, off):
         assert not held.any() or float(rel[held].max()) <= F32_G_RTOL, (name, float(rel[held].max()))
 
 
-def run(name, precision, insts, refs, weights=None):
+def run(name, precision, insts, refs, weights=None, f64_g_rtol=F64_G_RTOL):
     e = engine_for(insts, precision, weights)
     ll, g = e.logpdf_grad()
     off = e.grad_offsets()
     e.close()
-    check(name, precision, ll, g, refs, off)
+    check(name, precision, ll, g, refs, off, f64_g_rtol)
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
@@ -143,7 +148,7 @@ def test_config4_every_batched_instance(built_lib, precision):
     wins = _one("c4w", lambda: [window(b, min(b.S, 2000)) for b in simulate.hky_batch(
         seed=4, workers=min(16, os.cpu_count() or 1))])
     refs = _one("c4o", lambda: [oracle_scaled(w) for w in wins])
-    run("config4", precision, wins, refs)
+    run("config4", precision, wins, refs, f64_g_rtol=1e-9)
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32", "tf32x3", "tf32", "bf16"])

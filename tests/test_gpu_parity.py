@@ -163,6 +163,39 @@ def test_fp64_gradient_per_entry(built_lib, K, C, taxa, S, mf, model):
                                                                float(oracle_rel.max()))
 
 
+def test_fp64_gradient_short_branches(built_lib):
+    """Branches of length 1e-5 .. 1e-3 at slow rates: the reference's P(t) formula
+    U diag(exp) U^-1 cancels O(1) terms into O(t) off-diagonal entries there, so the
+    oracle (which follows it) loses up to ~1e-9; the engine's I + U diag(expm1) U^-1
+    does not.  Against an extended-precision evaluation the engine's FP64 gradient is
+    within 1e-12 relative per entry on entries with condition number <= 10, and never
+    further from it than the oracle."""
+    from extprec import ext_grad
+    if np.finfo(np.longdouble).eps >= np.finfo(np.float64).eps:
+        pytest.skip("longdouble is not wider than double here")
+    inst = random_instance(4, 4, 30, 400, seed=77)
+    rng = np.random.default_rng(78)
+    short = rng.choice(inst.N - 1, 12, replace=False)
+    inst.blen = inst.blen.copy()
+    inst.blen[short] = 10.0 ** rng.uniform(-5, -3, size=12)
+    inst.tree = T.from_parent(inst.parent, inst.blen)
+    llo, go = oracle(inst)
+    lle, ge, a = ext_grad(inst, with_scale=True)
+    ge, a = ge.astype(float), a.astype(float)
+    e = engine(inst, "f64")
+    e.set_sweep("walk")
+    ll, g = e.logpdf_grad()
+    e.close()
+    rel = np.abs(g - ge) / np.abs(ge)
+    orel = np.abs(go - ge) / np.abs(ge)
+    well = a / np.abs(ge) <= 10
+    print(f"\n[short branches] GPU max {rel.max():.2e} (well-conditioned {rel[well].max():.2e}) | "
+          f"oracle max {orel.max():.2e}")
+    assert abs(ll - float(lle)) <= 1e-12 * abs(float(lle))
+    assert well.any() and rel[well].max() <= 1e-12
+    assert rel.max() <= max(1e-12, orel.max())
+
+
 @pytest.mark.parametrize("sweep", ["walk", "level"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 def test_dense_leaf_values(built_lib, precision, sweep):
@@ -483,7 +516,10 @@ def test_device_entry_graph_replay_matches_eager(built_lib, precision):
             e.logpdf_device(d_l2.data_ptr())
             e.synchronize()
             out.append((ll, g, d_l2.cpu().numpy().copy()))
-        assert e.counts()["launches"] in (3, 4)
+        # one launch for the single-launch small-problem sweep, else record build,
+        # sweep and one or two reduction passes
+        assert e.counts()["launches"] == (1 if e.sweep() == "level" else 3) or \
+            e.counts()["launches"] == 4
         e.close()
         runs.append(out)
     for (ll0, g0, l0), (ll1, g1, l1) in zip(*runs):
