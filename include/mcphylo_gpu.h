@@ -187,6 +187,17 @@ int mcphy_synchronize(mcphy_handle h);
 /* Launch shape of the fused pruning kernel: sites per thread (1, 2 or 4) and
  * threads per block (64..256, multiple of 32); 0 keeps the automatic choice. */
 int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block);
+/* Rate categories per warp of the tree walk (no counterpart in the reference; its
+ * inner loop runs the categories of a site together, VectorizedFunctions.jl:195-210):
+ * 1 (default), 2 or 4 -- a thread's vector slots then hold sites_per_thread /
+ * rates_per_warp sites of that many categories, which share the sites' leaf-code
+ * loads and weights.  Honoured by the FP32 tree walk over table-row leaf codes with
+ * at most four states when it divides both sites_per_thread and the category count;
+ * elsewhere one category per warp.  0 keeps the automatic choice (1). */
+int mcphy_set_rates_per_warp(mcphy_handle h, int rates_per_warp);
+/* The launch shape of the current layout (laying it out first if needed): out3 =
+ * {sites_per_thread (vector slots per thread), threads_per_block, rates_per_warp}. */
+int mcphy_get_tiles(mcphy_handle h, int* out3);
 /* Sweep of the SIMT paths (no counterpart in the reference).
  *   MCPHY_SWEEP_WALK:  every warp walks the whole tree for its 32 x sites_per_thread
  *                      sites (throughput: many site blocks);
@@ -207,7 +218,8 @@ enum {
 int mcphy_set_sweep(mcphy_handle h, int sweep);
 int mcphy_get_sweep(mcphy_handle h, int* sweep);
 /* Picks the fused kernel's launch shape for the current problem: times each
- * candidate (sweep, sites per thread, threads per block) on full evaluations and
+ * candidate (sweep, sites per thread, threads per block, rate categories per warp)
+ * on full evaluations and
  * keeps the fastest (sweep and reduction time); out2 (may be NULL) receives sites
  * per thread and threads per block, mcphy_get_sweep the sweep.  No counterpart in the reference
  * (its @tturbo loops are tuned by LoopVectorization at compile time). */

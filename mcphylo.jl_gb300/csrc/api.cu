@@ -142,6 +142,7 @@ bool level_fits(const mcphy_engine* h, int tpb) {
 // Chooses the sweep and the launch shape.
 void choose_tiles(mcphy_engine* h) {
     h->sweep = MCPHY_SWEEP_WALK;
+    h->rpw = 1;
     if (tc_fmt(h) >= 0) {
         // one CTA of 128 threads per 128-site work item (4 x 32 sites)
         h->spt = 4;
@@ -185,9 +186,15 @@ void choose_tiles(mcphy_engine* h) {
     spt = std::min(spt, spt_max);
     if (spt != 1 && spt != 2 && spt != 4) spt = 1;
     h->spt = spt;
+    // several rate categories per warp: the row-code walk, FP32, up to four states,
+    // whole groups of categories in a thread's slots
+    const int rq = h->rpw_req;
+    if (rq > 1 && h->walk_rows && h->prec == MCPHY_PREC_F32 && h->Kp <= 4 && spt % rq == 0 &&
+        h->C % rq == 0)
+        h->rpw = rq;
     int tpb = h->tpb_req ? h->tpb_req : 128;
     // every warp owns two staging buffers of step records in shared memory
-    const int per_warp = walk_smem_per_warp(h->Kp, spt, int(real_size(h)), h->walk_rows);
+    const int per_warp = walk_smem_per_warp(h->Kp, spt, int(real_size(h)), h->walk_rows, h->rpw);
     const int max_warps = std::max(1, (200 * 1024) / per_warp);
     while (tpb / 32 > max_warps && tpb > 32) tpb -= 32;
     h->tpb = tpb;
@@ -216,8 +223,9 @@ int layout(mcphy_engine* h) {
         if (in.dense || in.ambig) h->walk_rows = false;
     }
     choose_tiles(h);
-    const int SB = 32 * h->spt;
+    const int SB = 32 * h->spt / h->rpw;   // sites of a work item
     const int K = h->K, Kp = h->Kp, C = h->C;
+    const int G = C / h->rpw;              // work items per site block (rate groups)
     h->desc.assign(h->M, InstanceDesc{});
     h->grad_offsets.assign(h->M + 1, 0);
     h->sched_all.clear();
@@ -293,7 +301,7 @@ int layout(mcphy_engine* h) {
         d.weight_off = w_off;
         w_off += d.S_pad;
         param_off += psize;
-        const int64_t items = int64_t(C) * d.n_blocks;
+        const int64_t items = int64_t(G) * d.n_blocks;
         item_off += items;
         pgrad_off += items * d.n_branch;
         blen_off += d.n_branch;
@@ -320,7 +328,7 @@ int layout(mcphy_engine* h) {
     int64_t ss = 0;
     for (int64_t i = 0; i < h->M; ++i) {
         const InstanceDesc& d = h->desc[i];
-        for (int64_t q = 0; q < int64_t(C) * d.n_blocks; ++q)
+        for (int64_t q = 0; q < int64_t(G) * d.n_blocks; ++q)
             items[d.item_off + q] = make_int2(int(i), int(q));
         for (int j = 0; j < d.J; ++j) steps[ss++] = make_int2(int(i), j);
     }
@@ -332,7 +340,7 @@ int layout(mcphy_engine* h) {
     queue.reserve(h->n_items);
     for (int64_t i : order) {
         const InstanceDesc& d = h->desc[i];
-        for (int64_t q = 0; q < int64_t(C) * d.n_blocks; ++q) queue.push_back(int32_t(d.item_off + q));
+        for (int64_t q = 0; q < int64_t(G) * d.n_blocks; ++q) queue.push_back(int32_t(d.item_off + q));
     }
 
     const size_t rs = real_size(h);
@@ -348,7 +356,7 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_blen, sizeof(double) * size_t(h->total_branch)))) return rc;
     if ((rc = ensure(h, h->d_pgrad, rs * size_t(pgrad_off)))) return rc;
     int64_t max_items = 0;
-    for (const InstanceDesc& d : h->desc) max_items = std::max<int64_t>(max_items, int64_t(C) * d.n_blocks);
+    for (const InstanceDesc& d : h->desc) max_items = std::max<int64_t>(max_items, int64_t(G) * d.n_blocks);
     h->n_split = int(std::min<int64_t>(64, std::max<int64_t>(1, (max_items + 127) / 128)));
     if ((rc = ensure(h, h->d_part, sizeof(double) * size_t(h->n_split) *
                                        size_t(h->M + h->total_branch))))
@@ -383,7 +391,7 @@ int layout(mcphy_engine* h) {
                      : level ? occupancy_prune_level(h->prec == MCPHY_PREC_F64, Kp, h->tpb, h->max_J, &bps)
                      : (h->prec == MCPHY_PREC_F64)
                          ? occupancy_prune_f64(Kp, h->spt, h->tpb, h->walk_rows, &bps)
-                         : occupancy_prune_f32(Kp, h->spt, h->tpb, h->walk_rows, &bps);
+                         : occupancy_prune_f32(Kp, h->spt, h->tpb, h->walk_rows, h->rpw, &bps);
     if (oe != cudaSuccess || bps < 1) bps = 1;
     // work items per CTA at a time: one per warp (tree walk), one per CTA otherwise;
     // scratch columns: per warp (tree walk) or per 128-thread CTA (tensor cores)
@@ -434,7 +442,7 @@ int gather_instance(mcphy_engine* h, int64_t i) {
                                         size_t(d.leaf_off) * cb);
     g.J = d.J;
     g.n_blocks = d.n_blocks;
-    g.slot_words = 32 * h->spt * cb / 4;
+    g.slot_words = 32 * (h->spt / h->rpw) * cb / 4;
     g.row_words = int64_t(d.S_pad) * cb / 4;
     CK(launch_gather_codes(g, h->stream));
     return MCPHY_OK;
@@ -558,6 +566,30 @@ int retopo(mcphy_engine* h) {
     return MCPHY_OK;
 }
 
+// M = U * Uinv (K x K, column-major), every entry the exact dot product of the FP64
+// inputs rounded once (double-double accumulation: the error of each product from
+// an FMA, of each sum from a two-sum).  With it the device forms the reference's
+// P(t) = U diag(exp(x)) Uinv as M + U diag(expm1(x)) Uinv: the same matrix (U Uinv is
+// the identity only up to rounding, and the reference's formula keeps that
+// residual), without cancelling O(1) terms into the O(t) entries of short branches.
+void unit_product(const double* U, const double* Ui, int K, double* M) {
+    for (int s = 0; s < K; ++s)
+        for (int k = 0; k < K; ++k) {
+            double hi = 0.0, lo = 0.0;
+            for (int m = 0; m < K; ++m) {
+                const double a = U[s + K * m], b = Ui[m + K * k];
+                const double p = a * b;
+                const double pe = std::fma(a, b, -p);   // a * b = p + pe exactly
+                const double t = hi + p;                 // two-sum of hi and p
+                const double bb = t - hi;
+                const double te = (hi - (t - bb)) + (p - bb);
+                hi = t;
+                lo += te + pe;
+            }
+            M[s + K * k] = hi + lo;
+        }
+}
+
 int upload_model(mcphy_engine* h) {
     const int K = h->K, Kp = h->Kp, C = h->C;
     const int64_t psize = param_size(K, Kp, C);
@@ -571,6 +603,7 @@ int upload_model(mcphy_engine* h) {
         p[2 * K * K + K] = in.mu;
         std::copy(in.rates.begin(), in.rates.end(), p + 2 * K * K + K + 1);
         std::copy(in.pi.begin(), in.pi.end(), p + 2 * K * K + K + 1 + C);
+        unit_product(in.U.data(), in.Uinv.data(), K, p + param_m_off(K, Kp, C));
     }
     CK(cudaMemcpy(h->d_params.p, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice));
     h->dirty &= ~unsigned(DIRTY_MODEL);
@@ -679,6 +712,7 @@ int run(mcphy_engine* h, bool want_grad) {
     b.Kp = h->Kp;
     b.C = h->C;
     b.counter = static_cast<int32_t*>(h->d_counter.p);   // zeroed for the sweep
+    b.rpw = h->rpw;
     const int fmt = tc_fmt(h);
     const bool tc = fmt >= 0;
     CK(tc ? launch_build_records_tc(fmt, b, st) : launch_build_records(f64, b, st));
@@ -714,13 +748,13 @@ int run(mcphy_engine* h, bool want_grad) {
     CK(tc    ? launch_prune_tc(fmt, h->K, h->blocks, a, st)
        : h->sweep == MCPHY_SWEEP_LEVEL ? launch_prune_level(f64, h->Kp, h->blocks, h->tpb, a, st)
        : f64 ? launch_prune_f64(h->Kp, h->spt, h->blocks, h->tpb, h->walk_rows, a, st)
-             : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, h->walk_rows, a, st));
+             : launch_prune_f32(h->Kp, h->spt, h->blocks, h->tpb, h->walk_rows, h->rpw, a, st));
     if (h->timing) CK(cudaEventRecord(h->ev[2], st));
 
     ReduceArgs r{};
     r.inst = b.inst;
     r.n_inst = int32_t(h->M);
-    r.C = h->C;
+    r.C = h->C / h->rpw;   // work items per site block
     r.n_split = h->n_split;
     r.want_grad = want_grad ? 1 : 0;
     r.total_branch = h->total_branch;
@@ -1249,6 +1283,25 @@ int mcphy_set_tiles(mcphy_handle h, int sites_per_thread, int threads_per_block)
     return MCPHY_OK;
 }
 
+int mcphy_set_rates_per_warp(mcphy_handle h, int rates_per_warp) {
+    if (!h) return MCPHY_ERR_ARG;
+    if (rates_per_warp != 0 && rates_per_warp != 1 && rates_per_warp != 2 && rates_per_warp != 4)
+        return fail(h, MCPHY_ERR_ARG, "rates_per_warp must be 0, 1, 2 or 4");
+    h->rpw_req = rates_per_warp;
+    h->dirty |= DIRTY_LAYOUT;
+    return MCPHY_OK;
+}
+
+int mcphy_get_tiles(mcphy_handle h, int* out3) {
+    if (!h || !out3) return MCPHY_ERR_ARG;
+    int rc;
+    if ((rc = prepare(h))) return rc;
+    out3[0] = h->spt;
+    out3[1] = h->tpb;
+    out3[2] = h->rpw;
+    return MCPHY_OK;
+}
+
 int mcphy_set_sweep(mcphy_handle h, int sweep) {
     if (!h) return MCPHY_ERR_ARG;
     if (sweep != MCPHY_SWEEP_AUTO && sweep != MCPHY_SWEEP_WALK && sweep != MCPHY_SWEEP_LEVEL)
@@ -1363,12 +1416,13 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
         return MCPHY_OK;
     }
     struct Cand {
-        int sweep, spt, tpb;
+        int sweep, spt, tpb, rpw;
     };
     std::vector<Cand> cand;
-    // tree-walk shapes (sites per thread, threads per block)
+    // tree-walk shapes (vector slots per thread, threads per block), one rate category
+    // per warp
     auto walk = [&](std::initializer_list<std::pair<int, int>> shapes) {
-        for (const auto& st : shapes) cand.push_back({MCPHY_SWEEP_WALK, st.first, st.second});
+        for (const auto& st : shapes) cand.push_back({MCPHY_SWEEP_WALK, st.first, st.second, 1});
     };
     if (h->prec == MCPHY_PREC_F64) {
         if (h->Kp <= 4) walk({{1, 128}, {2, 128}, {1, 64}, {2, 64}});
@@ -1385,23 +1439,32 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
         int rc0 = prepare(h);
         if (rc0) return rc0;
     }
+    // several rate categories per warp (row-code walk, FP32, up to four states):
+    // a thread's slots are sites x categories
+    if (h->walk_rows && h->prec == MCPHY_PREC_F32 && h->Kp <= 4) {
+        for (int q : {2, 4})
+            if (h->C % q == 0)
+                for (const auto& st : {std::make_pair(4, 128), std::make_pair(4, 64), std::make_pair(2, 128)})
+                    if (st.first % q == 0) cand.push_back({MCPHY_SWEEP_WALK, st.first, st.second, q});
+    }
     if (h->items_hint <= int64_t(8) * h->sm_count)
         for (int t : {64, 128, 256})
-            if (level_fits(h, t)) cand.push_back({MCPHY_SWEEP_LEVEL, 1, t});
+            if (level_fits(h, t)) cand.push_back({MCPHY_SWEEP_LEVEL, 1, t, 1});
     const bool timing = h->timing, graph = h->use_graph;
     h->timing = true;
     h->use_graph = false;
     float best = 1e30f;
-    int bw = h->sweep_req, bs = h->spt_req, bt = h->tpb_req;
+    int bw = h->sweep_req, bs = h->spt_req, bt = h->tpb_req, bq = h->rpw_req;
     int rc = MCPHY_OK;
     std::vector<double> ll(h->M), g(1);
     for (const Cand& c : cand) {
         h->sweep_req = c.sweep;
         h->spt_req = c.spt;
         h->tpb_req = c.tpb;
+        h->rpw_req = c.rpw;
         h->dirty |= DIRTY_LAYOUT;
         if ((rc = prepare(h))) break;
-        if (h->sweep != c.sweep) continue;   // did not fit
+        if (h->sweep != c.sweep || h->rpw != c.rpw) continue;   // did not fit
         if (g.size() < size_t(h->total_branch)) g.resize(h->total_branch);
         float t = 1e30f;
         for (int rep = 0; rep < 3 && rc == MCPHY_OK; ++rep) {
@@ -1416,6 +1479,7 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
             bw = c.sweep;
             bs = c.spt;
             bt = c.tpb;
+            bq = c.rpw;
         }
     }
     h->timing = timing;
@@ -1423,6 +1487,7 @@ int mcphy_autotune(mcphy_handle h, int* out2) {
     h->sweep_req = bw;
     h->spt_req = bs;
     h->tpb_req = bt;
+    h->rpw_req = bq;
     h->dirty |= DIRTY_LAYOUT;
     if (rc) return rc;
     if ((rc = prepare(h))) return rc;

@@ -59,8 +59,11 @@ struct mcphy_engine {
 
     // launch shape; sweep: MCPHY_SWEEP_WALK (a warp walks the whole tree) or
     // MCPHY_SWEEP_LEVEL (a CTA's warps share the tree level by level)
-    int spt_req = 0, tpb_req = 0, sweep_req = 0;
+    int spt_req = 0, tpb_req = 0, sweep_req = 0, rpw_req = 0;
     int spt = 1, tpb = 256, blocks = 0, sweep = 1;
+    // rate categories per warp of the row-code walk (1 elsewhere): a thread's spt
+    // vector slots hold spt / rpw sites of rpw categories
+    int rpw = 1;
     int32_t max_J_hint = 0;     // largest schedule, known before the layout (leaves - 1)
     // tree walk: the row-code kernel when every leaf of every instance is a table-row
     // code (no dense leaves, no partially ambiguous codes), else the general kernel;

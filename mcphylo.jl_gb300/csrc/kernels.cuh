@@ -192,7 +192,15 @@ struct BuildRecArgs {
     int32_t C;
     int32_t* counter;         // when set, thread 0 zeroes the sweep's work counter and
                               // error flag (the sweep runs after this kernel)
+    int32_t rpw;              // rate categories per warp of the tree walk: records are laid
+                              // out [rate group][step][rate in group] (1: [rate][step])
 };
+
+// Byte offset of the record of (rate r, step j) of an instance with J steps, for rate
+// groups of rpw categories: [r / rpw][j][r % rpw].
+__host__ __device__ inline size_t rec_index(int r, int j, int J, int rpw) {
+    return (size_t(r / rpw) * size_t(J) + size_t(j)) * size_t(rpw) + size_t(r % rpw);
+}
 
 struct ReduceArgs {
     const InstanceDesc* inst;
@@ -436,10 +444,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int li
 
 // Staging: chunk x of CH steps (records, and for code-leaf instances the leaf
 // codes of those steps) lives in buffer x & 1; one mbarrier per buffer.
-template <int KP, typename Real, int SPT, int CH_ = chunk_steps(KP, sizeof(Real))>
+// STEP_BYTES: records of one step (one rate's record, or the records of a group of
+// rate categories laid out side by side); TIP_BYTES: leaf codes of one step.
+template <int KP, typename Real, int SPT, int CH_ = chunk_steps(KP, sizeof(Real)),
+          int STEP_BYTES = rec_bytes(KP, sizeof(Real)), int TIP_BYTES = tip_bytes(KP, SPT)>
 struct Stage {
-    static constexpr int BYTES = rec_bytes(KP, sizeof(Real));
-    static constexpr int TIP = tip_bytes(KP, SPT);
+    static constexpr int BYTES = STEP_BYTES;
+    static constexpr int TIP = TIP_BYTES;
     static constexpr int CH = CH_;
     unsigned char* base;        // record buffer 0, record buffer 1, tip buffer 0, tip buffer 1
     uint64_t* bars;             // two mbarriers
@@ -1007,7 +1018,7 @@ template <typename Real>
 __device__ __forceinline__ void build_record_part(unsigned char* rec, const SchedNode& sn,
                                                   const SchedNode* sched, const InstanceDesc& d,
                                                   const double* params, const double* blen, int j,
-                                                  int K, int Kp, int r, int c, int s0, int R) {
+                                                  int K, int Kp, int C, int r, int c, int s0, int R) {
     if (c == 0 && s0 == 0) {
         int* hd = reinterpret_cast<int*>(rec);
         hd[0] = sn.op[0];
@@ -1047,11 +1058,13 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
     const double mu = Uinv[K * K];
     const double rate = Uinv[K * K + 1 + r];
     const double t = blen[d.blen_off + b];
-    // P = U diag(exp(x)) Uinv written as I + U diag(expm1(x)) Uinv: the same matrix,
-    // without the cancellation of O(1) terms that leaves the reference's formula
-    // (parallel_transition_prob, VectorizedFunctions.jl:155-168) with a relative error
-    // of up to ~1e-9 in the off-diagonal entries of short branches (t ~ 1e-5);
-    // dP/dt = U diag(D r mu exp(x)) Uinv as the reference forms it
+    // P = U diag(exp(x)) Uinv (parallel_transition_prob, VectorizedFunctions.jl:155-168)
+    // written as M + U diag(expm1(x)) Uinv with M = U Uinv rounded once (host,
+    // unit_product): the same matrix, without the cancellation of O(1) terms that
+    // leaves the reference's FP64 evaluation of it with a relative error of up to ~1e-9
+    // in the off-diagonal entries of short branches (t ~ 1e-5); dP/dt =
+    // U diag(D r mu exp(x)) Uinv as the reference forms it
+    const double* Mu = params + d.param_off + param_m_off(K, Kp, C);
     double em[32], de[32];
     if (s0 < K)
         for (int m = 0; m < K; ++m) {
@@ -1068,7 +1081,7 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
                     p += U[s + K * m] * em[m] * Uinv[m + K * k];
                     dp += U[s + K * m] * de[m] * Uinv[m + K * k];
                 }
-                if (s == k) p += 1.0;
+                p += Mu[s + K * k];
                 rs += p;
                 drs += dp;
             } else {
@@ -1100,8 +1113,8 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const InstanceDesc& d = a.inst[sj.x];
     const int j = sj.y;
     const SchedNode sn = a.sched[d.sched_off + j];
-    unsigned char* rec = a.recs + d.rec_off + (size_t(r) * d.J + j) * size_t(rec_bytes(Kp, sizeof(Real)));
-    build_record_part<Real>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, r, c, s0, R);
+    unsigned char* rec = a.recs + d.rec_off + rec_index(r, j, d.J, a.rpw) * size_t(rec_bytes(Kp, sizeof(Real)));
+    build_record_part<Real>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, C, r, c, s0, R);
 }
 
 // ---------------------------------------------------------------- reduction
@@ -1112,14 +1125,15 @@ constexpr int RY = 8;
 // Host-side launchers (defined per precision in kernels_f32.cu / kernels_f64.cu).
 // rows: the row-code tree walk (kernels_walk.cuh), for handles whose leaves are all
 // table-row codes; else the general tree walk above.
-cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
-                             cudaStream_t st);
+// rpw: rate categories per warp (row-code walk, FP32, Kp <= 4 only; else 1).
+cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, bool rows, int rpw,
+                             const PruneArgs& a, cudaStream_t st);
 cudaError_t launch_prune_f64(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
                              cudaStream_t st);
-cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, bool rows, int* blocks_per_sm);
+cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, bool rows, int rpw, int* blocks_per_sm);
 cudaError_t occupancy_prune_f64(int Kp, int spt, int tpb, bool rows, int* blocks_per_sm);
 // shared memory of one warp of the tree walk
-int walk_smem_per_warp(int Kp, int spt, int real_bytes, bool rows);
+int walk_smem_per_warp(int Kp, int spt, int real_bytes, bool rows, int rpw);
 
 // Level-synchronous sweep for small trees (kernels_level.cu): a CTA of tpb threads
 // owns one 32-site work item at a time; its warps share the tree level by level.

@@ -3,17 +3,17 @@
 
 namespace mcphy {
 
-cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
-                             cudaStream_t st) {
-    return PruneLaunch<float>::launch(Kp, spt, blocks, tpb, rows, a, st);
+cudaError_t launch_prune_f32(int Kp, int spt, int blocks, int tpb, bool rows, int rpw,
+                             const PruneArgs& a, cudaStream_t st) {
+    return PruneLaunch<float>::launch(Kp, spt, blocks, tpb, rows, rpw, a, st);
 }
 
-cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, bool rows, int* bps) {
-    return PruneLaunch<float>::occupancy(Kp, spt, tpb, rows, bps);
+cudaError_t occupancy_prune_f32(int Kp, int spt, int tpb, bool rows, int rpw, int* bps) {
+    return PruneLaunch<float>::occupancy(Kp, spt, tpb, rows, rpw, bps);
 }
 
-int walk_smem_per_warp(int Kp, int spt, int real_bytes, bool rows) {
-    return rows ? walk_warp_smem_bytes(Kp, spt, real_bytes) : warp_smem_bytes(Kp, spt, real_bytes);
+int walk_smem_per_warp(int Kp, int spt, int real_bytes, bool rows, int rpw) {
+    return rows ? walk_warp_smem_bytes(Kp, spt, real_bytes, rpw) : warp_smem_bytes(Kp, spt, real_bytes);
 }
 
 }  // namespace mcphy

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
                 for (int q = threadIdx.x; q < J * 2 * R; q += blockDim.x) {
                     const int s0 = q % R, c = (q / R) % 2, j = q / (2 * R);
                     build_record_part<Real>(srec + size_t(j) * RB, sc[j], sc, d, a.params, a.blen, j,
-                                            a.K, KP, r, c, s0, R);
+                                            a.K, KP, C, r, c, s0, R);
                 }
             } else {
                 const int4* src = reinterpret_cast<const int4*>(a.recs + d.rec_off + size_t(r) * J * RB);

@@ -123,9 +123,11 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
     };
     const int b = sn.br[c];
     const bool real = b < d.n_branch;
-    // P = I + U diag(expm1(x)) Uinv (see build_record_part, kernels.cuh)
+    // P = M + U diag(expm1(x)) Uinv, M = U Uinv rounded once (see build_record_part,
+    // kernels.cuh)
     double em[32], de[32];
     const double* U = a.params + d.param_off;
+    const double* Mu = U + param_m_off(K, a.Kp, C);
     const double* Uinv = U + K * K + K;
     if (real && s < K) {
         const double* Dv = U + K * K;
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
                     p += U[s + K * m] * em[m] * Uinv[m + K * k];
                     dp += U[s + K * m] * de[m] * Uinv[m + K * k];
                 }
-                if (s == k) p += 1.0;
+                p += Mu[s + K * k];
             } else {
                 p = (s == k) ? 1.0 : 0.0;
             }

@@ -21,17 +21,22 @@
 
 namespace mcphy {
 
+// Rate categories per warp (RPW): a thread's SPT vector slots hold SPT / RPW sites of
+// RPW rate categories (slot u: site u % (SPT / RPW), category u / (SPT / RPW)), so the
+// warp loads each leaf code and site weight once for all its categories; a step's
+// records are the RPW categories' records side by side (rec_index, kernels.cuh).
 // steps per staged chunk of the row-code walk: the largest power of two with at most
 // 3 KB of records per buffer (at least 1)
-__host__ __device__ constexpr int walk_chunk_steps(int kp, int real_bytes) {
-    return rec_bytes(kp, real_bytes) > 1536   ? 1
-           : rec_bytes(kp, real_bytes) > 768  ? 2
-           : rec_bytes(kp, real_bytes) > 384  ? 4
-           : rec_bytes(kp, real_bytes) > 192  ? 8
-                                              : 16;
+__host__ __device__ constexpr int walk_chunk_steps(int kp, int real_bytes, int rpw = 1) {
+    return rpw * rec_bytes(kp, real_bytes) > 1536   ? 1
+           : rpw * rec_bytes(kp, real_bytes) > 768  ? 2
+           : rpw * rec_bytes(kp, real_bytes) > 384  ? 4
+           : rpw * rec_bytes(kp, real_bytes) > 192  ? 8
+                                                    : 16;
 }
-__host__ __device__ constexpr int walk_warp_smem_bytes(int kp, int spt, int real_bytes) {
-    return (2 * walk_chunk_steps(kp, real_bytes) * (rec_bytes(kp, real_bytes) + tip_bytes(kp, spt)) +
+__host__ __device__ constexpr int walk_warp_smem_bytes(int kp, int spt, int real_bytes, int rpw = 1) {
+    return (2 * walk_chunk_steps(kp, real_bytes, rpw) *
+                (rpw * rec_bytes(kp, real_bytes) + tip_bytes(kp, spt / rpw)) +
             stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 + 127) /
            128 * 128;
 }
@@ -50,6 +55,45 @@ __device__ __forceinline__ void lookup(const Real* T, const uint32_t (&c)[SPT], 
 #pragma unroll
     for (int u = 0; u < SPT; ++u) ld_vec<KP>(T + c[u] * KP, D[u]);
 }
+
+// Per-category forms (RPW > 1): slot u uses the table `which` of category u / SPS's
+// record (rj + (u / SPS) * RB) and site u % SPS's code.  The operation order per
+// slot is the RPW = 1 forms', row by row.
+template <int KP, int SPT, int SPS, typename Real>
+__device__ __forceinline__ void lookup_q(const unsigned char* rj, int RB, int which,
+                                         const uint32_t (&c)[SPS], Real (&D)[SPT][KP]) {
+#pragma unroll
+    for (int u = 0; u < SPT; ++u)
+        ld_vec<KP>(rec_mat_ptr<KP, Real>(rj + (u / SPS) * RB, which) + c[u % SPS] * KP, D[u]);
+}
+template <int KP, int SPT, int SPS, typename Real>
+__device__ __forceinline__ void apply_t_q(const unsigned char* rj, int RB, int which,
+                                          const Real (&L)[SPT][KP], Real (&D)[SPT][KP]) {
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) {
+        const Real* T = rec_mat_ptr<KP, Real>(rj + (u / SPS) * RB, which);
+        Real Lu[1][KP], Du[1][KP];
+#pragma unroll
+        for (int k = 0; k < KP; ++k) Lu[0][k] = L[u][k];
+        apply_t<KP, 1>(T, Lu, Du);
+#pragma unroll
+        for (int k = 0; k < KP; ++k) D[u][k] = Du[0][k];
+    }
+}
+template <int KP, int SPT, int SPS, typename Real>
+__device__ __forceinline__ void apply_tt_q(const unsigned char* rj, int RB, int which,
+                                           const Real (&x)[SPT][KP], Real (&y)[SPT][KP]) {
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) {
+        const Real* T = rec_mat_ptr<KP, Real>(rj + (u / SPS) * RB, which);
+        Real xu[1][KP], yu[1][KP];
+#pragma unroll
+        for (int k = 0; k < KP; ++k) xu[0][k] = x[u][k];
+        apply_tt<KP, 1>(T, xu, yu);
+#pragma unroll
+        for (int k = 0; k < KP; ++k) y[u][k] = yu[0][k];
+    }
+}
 // L = X * Y elementwise
 template <int KP, int SPT, typename Real>
 __device__ __forceinline__ void vmul(Real (&L)[SPT][KP], const Real (&X)[SPT][KP], const Real (&Y)[SPT][KP]) {
@@ -65,10 +109,13 @@ __device__ __forceinline__ void vmul(Real (&L)[SPT][KP], const Real (&X)[SPT][KP
     }
 }
 
-template <int KP, typename Real, int SPT>
+template <int KP, typename Real, int SPT, int RPW = 1>
 __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
-    constexpr int CH = walk_chunk_steps(KP, sizeof(Real));
-    using St = Stage<KP, Real, SPT, CH>;
+    static_assert(SPT % RPW == 0, "the vector slots hold whole groups of categories");
+    constexpr int SPS = SPT / RPW;                  // sites per thread
+    constexpr int RB = rec_bytes(KP, sizeof(Real)); // one category's record
+    constexpr int CH = walk_chunk_steps(KP, sizeof(Real), RPW);
+    using St = Stage<KP, Real, SPT, CH, RPW * RB, tip_bytes(KP, SPS)>;
     constexpr int NS = stack_smem_slots(KP, SPT, sizeof(Real));
     constexpr int SLOT = SPT * 32 * KP;             // Real elements per warp vector
     extern __shared__ __align__(128) unsigned char smem[];
@@ -80,7 +127,7 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
     const int C = a.C;
     constexpr double LN2 = 0.6931471805599453094;
 
-    unsigned char* wbase = smem + size_t(wib) * walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)));
+    unsigned char* wbase = smem + size_t(wib) * walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)), RPW);
     Real* sstack = reinterpret_cast<Real*>(wbase + 2 * CH * (St::BYTES + St::TIP));
     uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
                                                   NS * SLOT * sizeof(Real));
@@ -92,6 +139,20 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
     auto stack_ptr = [&](int s) -> Real* {
         return s < NS ? sstack + s * SLOT : gstack + int64_t(s) * SLOT;
     };
+    // table `which` of step record rj applied to the warp's slots (per category
+    // when a warp holds several)
+    auto look = [&](const unsigned char* rj, int which, const uint32_t (&c)[SPS], Real (&D)[SPT][KP]) {
+        if constexpr (RPW == 1) lookup<KP, SPT>(rec_mat_ptr<KP, Real>(rj, which), c, D);
+        else lookup_q<KP, SPT, SPS>(rj, RB, which, c, D);
+    };
+    auto mat = [&](const unsigned char* rj, int which, const Real (&L)[SPT][KP], Real (&D)[SPT][KP]) {
+        if constexpr (RPW == 1) apply_t<KP, SPT>(rec_mat_ptr<KP, Real>(rj, which), L, D);
+        else apply_t_q<KP, SPT, SPS>(rj, RB, which, L, D);
+    };
+    auto mat_t = [&](const unsigned char* rj, int which, const Real (&x)[SPT][KP], Real (&y)[SPT][KP]) {
+        if constexpr (RPW == 1) apply_tt<KP, SPT>(rec_mat_ptr<KP, Real>(rj, which), x, y);
+        else apply_tt_q<KP, SPT, SPS>(rj, RB, which, x, y);
+    };
 
     for (;;) {
         int t = 0;
@@ -101,17 +162,19 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
         const int item = __ldg(a.queue + t);
         const int2 it = __ldg(a.items + item);
         const InstanceDesc d = a.inst[it.x];
-        const int r = it.y / d.n_blocks;
+        const int r = it.y / d.n_blocks;          // rate category (group of RPW categories)
         const int blk = it.y - r * d.n_blocks;
-        const int site0 = blk * (32 * SPT) + lane;
+        const int site0 = blk * (32 * SPS) + lane;
         const double* pi_d = a.params + d.param_off + 2 * a.K * a.K + a.K + 1 + C;
         const int J = d.J;
 
         // site-pattern weights of the gradient terms, 0 past the last site
         Real wtr[SPT];
 #pragma unroll
-        for (int u = 0; u < SPT; ++u)
-            wtr[u] = (site0 + 32 * u) < d.S ? Real(__ldg(a.weights + d.weight_off + site0 + 32 * u)) : Real(0);
+        for (int u = 0; u < SPT; ++u) {
+            const int site = site0 + 32 * (u % SPS);
+            wtr[u] = site < d.S ? Real(__ldg(a.weights + d.weight_off + site)) : Real(0);
+        }
 
         st.src = a.recs + d.rec_off + size_t(r) * size_t(J) * St::BYTES;
         st.tsrc = reinterpret_cast<const unsigned char*>(a.codes) + d.leaf_off +
@@ -137,20 +200,20 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
             if (h[0] >= 0) {
                 Real A[SPT][KP];
                 read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
-                apply_t<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 0), A, D0);
+                mat(rj, 0, A, D0);
             } else {
-                uint32_t c[SPT];
-                read_rows<KP, SPT>(st.tip(j, 0), lane, c);
-                lookup<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 0), c, D0);
+                uint32_t c[SPS];
+                read_rows<KP, SPS>(st.tip(j, 0), lane, c);
+                look(rj, 0, c, D0);
             }
             {
                 Real D1[SPT][KP];
                 if (h[1] >= 0) {
-                    apply_t<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 2), Lp, D1);
+                    mat(rj, 2, Lp, D1);
                 } else {
-                    uint32_t c[SPT];
-                    read_rows<KP, SPT>(st.tip(j, 1), lane, c);
-                    lookup<KP, SPT>(rec_mat_ptr<KP, Real>(rj, 2), c, D1);
+                    uint32_t c[SPS];
+                    read_rows<KP, SPS>(st.tip(j, 1), lane, c);
+                    look(rj, 2, c, D1);
                 }
                 vmul<KP, SPT>(Lp, D0, D1);
             }
@@ -167,8 +230,9 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                     for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Lp[u][k], lik);
                     const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
                     const double v = log_site(lik) + double(ex) * LN2;
-                    const bool valid = (site0 + 32 * u) < d.S;
-                    const double w = valid ? __ldg(a.weights + d.weight_off + site0 + 32 * u) : 0.0;
+                    const int site = site0 + 32 * (u % SPS);
+                    const bool valid = site < d.S;
+                    const double w = valid ? __ldg(a.weights + d.weight_off + site) : 0.0;
                     ll_lane += valid ? w * v : 0.0;
                 }
             }
@@ -214,9 +278,9 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 if (pf.y >= 0) prefetch_l2(post + int64_t(pf.y) * SLOT, SLOT * sizeof(Real));
             }
             if (h[3] >= 0) read_vec<KP, SPT>(stack_ptr(h[3]), lane, pb);   // else carried
-            uint32_t c0[SPT], c1[SPT];
-            if (h[0] < 0) read_rows<KP, SPT>(st.tip(j, 0), lane, c0);
-            if (h[1] < 0) read_rows<KP, SPT>(st.tip(j, 1), lane, c1);
+            uint32_t c0[SPS], c1[SPS];
+            if (h[0] < 0) read_rows<KP, SPS>(st.tip(j, 0), lane, c0);
+            if (h[1] < 0) read_rows<KP, SPS>(st.tip(j, 1), lane, c1);
             // operands of the next step, one step ahead
             if (j > 0) {
                 const int qn = (j - 1) / CH;
@@ -228,13 +292,11 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, Y0);
                 if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, Y1);
             }
-            const Real* P0 = rec_mat_ptr<KP, Real>(rj, 0);
-            const Real* P1 = rec_mat_ptr<KP, Real>(rj, 2);
             Real D0[SPT][KP], D1[SPT][KP];
-            if (h[0] >= 0) apply_t<KP, SPT>(P0, X0, D0);
-            else lookup<KP, SPT>(P0, c0, D0);
-            if (h[1] >= 0) apply_t<KP, SPT>(P1, X1, D1);
-            else lookup<KP, SPT>(P1, c1, D1);
+            if (h[0] >= 0) mat(rj, 0, X0, D0);
+            else look(rj, 0, c0, D0);
+            if (h[1] >= 0) mat(rj, 2, X1, D1);
+            else look(rj, 2, c1, D1);
             Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
             // wide state spaces: the gradient ratio's denominator pt_c . D_c =
             // sum_k pb_k D0_k D1_k is the same for both children, computed once
@@ -260,9 +322,8 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 }
                 if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
-                    const Real* dP = rec_mat_ptr<KP, Real>(rj, 2 * c + 1);
-                    if (h[c] >= 0) apply_t<KP, SPT>(dP, c == 0 ? X0 : X1, dD);
-                    else lookup<KP, SPT>(dP, c == 0 ? c0 : c1, dD);
+                    if (h[c] >= 0) mat(rj, 2 * c + 1, c == 0 ? X0 : X1, dD);
+                    else look(rj, 2 * c + 1, c == 0 ? c0 : c1, dD);
                     Real g = Real(0);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
@@ -289,11 +350,11 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                     uint32_t unused[SPT] = {};
                     if (c == 1) {
                         // child 1 is the next step: its pre-order partial is the next pb
-                        apply_tt<KP, SPT>(P1, pt, pb);
+                        mat_t(rj, 2, pt, pb);
                         rescale_warp<KP, Real, SPT>(pb, unused);
                     } else {
                         Real pbc[SPT][KP];
-                        apply_tt<KP, SPT>(P0, pt, pbc);
+                        mat_t(rj, 0, pt, pbc);
                         rescale_warp<KP, Real, SPT>(pbc, unused);
                         write_vec<KP, SPT>(stack_ptr(h[2]), lane, pbc);
                     }

@@ -176,7 +176,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     const bool f64 = h->prec == MCPHY_PREC_F64;
     const size_t rs = f64 ? 8 : 4;
     int64_t pgrad_elems = 0;
-    for (const InstanceDesc& d : h->desc) pgrad_elems += int64_t(h->C) * d.n_blocks * d.n_branch;
+    for (const InstanceDesc& d : h->desc) pgrad_elems += int64_t(h->C / h->rpw) * d.n_blocks * d.n_branch;
     const size_t n_out = size_t(h->M + h->total_branch);
 
     // carve the fixed array: counter | item ll | split sums | results | item grads | warps
@@ -225,6 +225,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     b.K = h->K;
     b.Kp = h->Kp;
     b.C = h->C;
+    b.rpw = h->rpw;
     NA_CK(launch_build_records(f64, b, st));
 
     // work counter and error flag start at zero on every call
@@ -259,12 +260,12 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     a.max_J = h->max_J;
     NA_CK(h->sweep == MCPHY_SWEEP_LEVEL ? launch_prune_level(f64, h->Kp, int(blocks), h->tpb, a, st)
           : f64 ? launch_prune_f64(h->Kp, h->spt, int(blocks), h->tpb, h->walk_rows, a, st)
-                : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, h->walk_rows, a, st));
+                : launch_prune_f32(h->Kp, h->spt, int(blocks), h->tpb, h->walk_rows, h->rpw, a, st));
 
     ReduceArgs r{};
     r.inst = b.inst;
     r.n_inst = int32_t(h->M);
-    r.C = h->C;
+    r.C = h->C / h->rpw;   // work items per site block
     r.n_split = h->n_split;
     r.want_grad = 1;
     r.total_branch = h->total_branch;

@@ -20,49 +20,67 @@ __host__ __device__ constexpr int walk_spt_max(int kp, int real_bytes) {
 
 template <typename Real>
 struct PruneLaunch {
-    template <int KP, int SPT, bool ROWS>
+    template <int KP, int SPT, bool ROWS, int RPW>
     static const void* kernel() {
-        if constexpr (ROWS) return reinterpret_cast<const void*>(&prune_rows_kernel<KP, Real, SPT>);
+        if constexpr (ROWS) return reinterpret_cast<const void*>(&prune_rows_kernel<KP, Real, SPT, RPW>);
         else return reinterpret_cast<const void*>(&prune_kernel<KP, Real, SPT>);
     }
-    template <int KP, int SPT, bool ROWS>
+    template <int KP, int SPT, bool ROWS, int RPW>
     static SmemAllowance& allowance() {
         static SmemAllowance a;
         return a;
     }
-    template <int KP, int SPT, bool ROWS>
+    template <int KP, int SPT, bool ROWS, int RPW>
     static cudaError_t allow(int smem) {
-        return raise_smem(allowance<KP, SPT, ROWS>(), smem, [](int bytes) {
-            return cudaFuncSetAttribute(kernel<KP, SPT, ROWS>(), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        bytes);
+        return raise_smem(allowance<KP, SPT, ROWS, RPW>(), smem, [](int bytes) {
+            return cudaFuncSetAttribute(kernel<KP, SPT, ROWS, RPW>(),
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         });
     }
-    template <int KP, int SPT, bool ROWS>
+    template <int KP, int SPT, bool ROWS, int RPW>
     static int smem_of(int tpb) {
-        return (tpb / 32) * (ROWS ? walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)))
+        return (tpb / 32) * (ROWS ? walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)), RPW)
                                   : warp_smem_bytes(KP, SPT, int(sizeof(Real))));
     }
-    template <int KP, int SPT, bool ROWS>
+    template <int KP, int SPT, bool ROWS, int RPW>
     static cudaError_t go(int blocks, int tpb, const PruneArgs& a, cudaStream_t st) {
-        const int smem = smem_of<KP, SPT, ROWS>(tpb);
-        cudaError_t e = allow<KP, SPT, ROWS>(smem);
+        const int smem = smem_of<KP, SPT, ROWS, RPW>(tpb);
+        cudaError_t e = allow<KP, SPT, ROWS, RPW>(smem);
         if (e != cudaSuccess) return e;
-        if constexpr (ROWS) prune_rows_kernel<KP, Real, SPT><<<blocks, tpb, smem, st>>>(a);
+        if constexpr (ROWS) prune_rows_kernel<KP, Real, SPT, RPW><<<blocks, tpb, smem, st>>>(a);
         else prune_kernel<KP, Real, SPT><<<blocks, tpb, smem, st>>>(a);
         return cudaGetLastError();
     }
-    template <int KP, int SPT, bool ROWS>
+    template <int KP, int SPT, bool ROWS, int RPW>
     static cudaError_t occ(int tpb, int* bps) {
-        const int smem = smem_of<KP, SPT, ROWS>(tpb);
+        const int smem = smem_of<KP, SPT, ROWS, RPW>(tpb);
         // the largest block a later launch may use (8 warps), so that launches need
         // not raise it again; where that does not fit, the block asked for
-        cudaError_t e = allow<KP, SPT, ROWS>(std::max(smem, smem_of<KP, SPT, ROWS>(256)));
+        cudaError_t e = allow<KP, SPT, ROWS, RPW>(std::max(smem, smem_of<KP, SPT, ROWS, RPW>(256)));
         if (e != cudaSuccess) {
             cudaGetLastError();
-            e = allow<KP, SPT, ROWS>(smem);
+            e = allow<KP, SPT, ROWS, RPW>(smem);
         }
         if (e != cudaSuccess) return e;
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, kernel<KP, SPT, ROWS>(), tpb, smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, kernel<KP, SPT, ROWS, RPW>(), tpb, smem);
+    }
+    // rate categories per warp: instantiated for FP32 at up to four states; other
+    // shapes run with one category per warp
+    static constexpr bool rpw_ok(int kp) { return sizeof(Real) == 4 && kp <= 4; }
+    template <int KP, int SPT, typename F>
+    static cudaError_t by_rpw(bool rows, int rpw, F&& f) {
+        if (!rows) return f(std::integral_constant<int, KP>(), std::integral_constant<int, SPT>(),
+                            std::false_type(), std::integral_constant<int, 1>());
+        if constexpr (rpw_ok(KP) && SPT % 4 == 0)
+            if (rpw == 4)
+                return f(std::integral_constant<int, KP>(), std::integral_constant<int, SPT>(),
+                         std::true_type(), std::integral_constant<int, 4>());
+        if constexpr (rpw_ok(KP) && SPT % 2 == 0)
+            if (rpw == 2)
+                return f(std::integral_constant<int, KP>(), std::integral_constant<int, SPT>(),
+                         std::true_type(), std::integral_constant<int, 2>());
+        return f(std::integral_constant<int, KP>(), std::integral_constant<int, SPT>(), std::true_type(),
+                 std::integral_constant<int, 1>());
     }
 
     // f(integral_constant KP, integral_constant SPT) for the instantiated shapes;
@@ -85,17 +103,21 @@ struct PruneLaunch {
             default: return cudaErrorInvalidValue;
         }
     }
-    static cudaError_t launch(int Kp, int spt, int blocks, int tpb, bool rows, const PruneArgs& a,
+    static cudaError_t launch(int Kp, int spt, int blocks, int tpb, bool rows, int rpw, const PruneArgs& a,
                               cudaStream_t st) {
         return dispatch(Kp, spt, [&](auto kp, auto s) {
-            constexpr int K_ = decltype(kp)::value, S_ = decltype(s)::value;
-            return rows ? go<K_, S_, true>(blocks, tpb, a, st) : go<K_, S_, false>(blocks, tpb, a, st);
+            return by_rpw<decltype(kp)::value, decltype(s)::value>(rows, rpw, [&](auto k2, auto s2, auto r2, auto q2) {
+                return go<decltype(k2)::value, decltype(s2)::value, decltype(r2)::value, decltype(q2)::value>(
+                    blocks, tpb, a, st);
+            });
         });
     }
-    static cudaError_t occupancy(int Kp, int spt, int tpb, bool rows, int* bps) {
+    static cudaError_t occupancy(int Kp, int spt, int tpb, bool rows, int rpw, int* bps) {
         return dispatch(Kp, spt, [&](auto kp, auto s) {
-            constexpr int K_ = decltype(kp)::value, S_ = decltype(s)::value;
-            return rows ? occ<K_, S_, true>(tpb, bps) : occ<K_, S_, false>(tpb, bps);
+            return by_rpw<decltype(kp)::value, decltype(s)::value>(rows, rpw, [&](auto k2, auto s2, auto r2, auto q2) {
+                return occ<decltype(k2)::value, decltype(s2)::value, decltype(r2)::value, decltype(q2)::value>(
+                    tpb, bps);
+            });
         });
     }
 };

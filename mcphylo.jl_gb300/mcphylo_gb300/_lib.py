@@ -69,6 +69,8 @@ SIGNATURES = {
     "mcphy_enable_graph": (c_int, [handle_t, c_int]),
     "mcphy_debug_inject": (c_int, [handle_t, c_int]),
     "mcphy_debug_check_allowance": (c_int, []),
+    "mcphy_set_rates_per_warp": (c_int, [handle_t, c_int]),
+    "mcphy_get_tiles": (c_int, [handle_t, P(c_int)]),
     "mcphy_enable_timing": (c_int, [handle_t, c_int]),
     "mcphy_get_timing": (c_int, [handle_t, P(ctypes.c_float)]),
     "mcphy_get_counts": (c_int, [handle_t, pi64]),

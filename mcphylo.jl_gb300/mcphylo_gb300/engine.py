@@ -140,6 +140,17 @@ class Engine:
         check(self._L.mcphy_set_tiles(self._h, sites_per_thread, threads_per_block), self._h,
               "set_tiles")
 
+    def set_rates_per_warp(self, rates_per_warp: int = 0) -> None:
+        """Rate categories per warp of the FP32 tree walk (1, 2 or 4; 0: automatic)."""
+        check(self._L.mcphy_set_rates_per_warp(self._h, int(rates_per_warp)), self._h,
+              "set_rates_per_warp")
+
+    def tiles(self):
+        """(sites_per_thread, threads_per_block, rates_per_warp) of the current layout."""
+        out = (ctypes.c_int * 3)()
+        check(self._L.mcphy_get_tiles(self._h, out), self._h, "get_tiles")
+        return int(out[0]), int(out[1]), int(out[2])
+
     SWEEPS = {"auto": 0, "walk": 1, "level": 2}
 
     def set_sweep(self, sweep: str = "auto") -> None:
