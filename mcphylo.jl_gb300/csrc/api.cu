@@ -604,6 +604,17 @@ int upload_model(mcphy_engine* h) {
         std::copy(in.rates.begin(), in.rates.end(), p + 2 * K * K + K + 1);
         std::copy(in.pi.begin(), in.pi.end(), p + 2 * K * K + K + 1 + C);
         unit_product(in.U.data(), in.Uinv.data(), K, p + param_m_off(K, Kp, C));
+        // Q_r = U diag(D rate_r mu) Uinv: dP/dt = Q_r P, so a gradient term's dP L is Q_r D
+        for (int r = 0; r < C; ++r) {
+            double* Q = p + param_q_off(K, Kp, C) + int64_t(r) * K * K;
+            for (int s2 = 0; s2 < K; ++s2)
+                for (int k = 0; k < K; ++k) {
+                    double q = 0.0;
+                    for (int m = 0; m < K; ++m)
+                        q += in.U[s2 + K * m] * (in.D[m] * in.rates[r] * in.mu) * in.Uinv[m + K * k];
+                    Q[s2 + K * k] = q;
+                }
+        }
     }
     CK(cudaMemcpy(h->d_params.p, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice));
     h->dirty &= ~unsigned(DIRTY_MODEL);

@@ -78,10 +78,12 @@ __host__ __device__ constexpr int tip_bytes(int kp, int spt) { return 2 * 32 * s
 __host__ __device__ constexpr int stack_smem_slots(int kp, int spt, int real_bytes) {
     return vec_bytes(kp, spt, real_bytes) <= 1024 ? 6 : vec_bytes(kp, spt, real_bytes) <= 4096 ? 3 : 1;
 }
-// rounded to 128 bytes so every warp's TMA destinations stay aligned
+// plus the transposed scaled rate matrix Q_r^T (kp x kp); rounded to 128 bytes so
+// every warp's TMA destinations stay aligned
 __host__ __device__ constexpr int warp_smem_bytes(int kp, int spt, int real_bytes) {
     return (2 * chunk_steps(kp, real_bytes) * (rec_bytes(kp, real_bytes) + tip_bytes(kp, spt)) +
-            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 + 127) /
+            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) +
+            kp * kp * real_bytes + 16 + 127) /
            128 * 128;
 }
 
@@ -728,8 +730,8 @@ prune_kernel(const PruneArgs a) {
 
     unsigned char* wbase = smem + size_t(wib) * warp_smem_bytes(KP, SPT, int(sizeof(Real)));
     Real* sstack = reinterpret_cast<Real*>(wbase + 2 * CH * (St::BYTES + St::TIP));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
-                                                  NS * SLOT * sizeof(Real));
+    Real* sq = sstack + NS * SLOT;   // Q_r^T of the current rate category, KP x KP
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sq + KP * KP);
     St st;
     st.init(wbase, bars, lane, a.wait_limit, a.inject_timeout != 0);
     if (lane == 0) fence_mbar_init();
@@ -785,11 +787,22 @@ prune_kernel(const PruneArgs a) {
                               : nullptr;
         st.J = J;
         st.Q = (J + CH - 1) / CH;
+        if (a.want_grad) {
+            // Q_r^T: sq[k][s] = Q_r[s][k], zero padded (dP/dt = Q_r P)
+            const double* Qp = a.params + d.param_off + param_q_off(a.K, KP, C) + int64_t(r) * a.K * a.K;
+            for (int e = lane; e < KP * KP; e += 32) {
+                const int k = e / KP, s2 = e % KP;
+                sq[e] = (s2 < a.K && k < a.K) ? Real(__ldg(Qp + s2 + a.K * k)) : Real(0);
+            }
+        }
         __syncwarp();
         st.issue(0, lane);
         if (st.Q > 1) st.issue(1, lane);
 
         // ---------------- post-order sweep (logL)
+        // the post-order column keeps, for every internal child, its Down vector
+        // D_c = P_c L_c (read back by the gradient sweep instead of recomputed; dP L
+        // is formed there as Q_r D)
         uint32_t eacc[SPT];
 #pragma unroll
         for (int u = 0; u < SPT; ++u) eacc[u] = 0u;
@@ -808,6 +821,10 @@ prune_kernel(const PruneArgs a) {
             Real Da[SPT][KP], Db[SPT][KP];
             down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), Da);
             down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), Db);
+            if (a.want_grad) {
+                if (h[0] >= 0) write_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, Da);
+                if (h[1] >= 0) write_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, Db);
+            }
 #pragma unroll
             for (int u = 0; u < SPT; ++u) {
                 if constexpr (Pairs<Real, KP>::value) {
@@ -821,8 +838,6 @@ prune_kernel(const PruneArgs a) {
             }
             rescale_warp<KP, Real, SPT>(Da, eacc);
             if (j + 1 < J) {
-                // the post-order column is only read back by the gradient sweep
-                if (a.want_grad) write_vec<KP, SPT>(post + int64_t(j) * SLOT, lane, Da);
                 if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Da);
                 copy_part(Lp, Da);
             } else {
@@ -895,9 +910,12 @@ prune_kernel(const PruneArgs a) {
                 if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, NA);
                 if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, NB);
             }
+            // internal children: A / B are their stored Down vectors
             Real D[2][SPT][KP];
-            down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 0), D[0]);
-            down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
+            if (h[0] >= 0) copy_part(D[0], A);
+            else down<KP, SPT>(A, code_leaves, ambig, rec_mat_ptr<KP, Real>(rj, 0), D[0]);
+            if (h[1] >= 0) copy_part(D[1], B);
+            else down<KP, SPT>(B, code_leaves, ambig, rec_mat_ptr<KP, Real>(rj, 2), D[1]);
             Real Npb[SPT][KP];
             Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
             // wide state spaces: the gradient ratio's denominator pt_c . D_c =
@@ -935,8 +953,9 @@ prune_kernel(const PruneArgs a) {
                 }
                 if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
-                    if (c == 0) down<KP, SPT>(A, code_leaves && h[0] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
-                    else down<KP, SPT>(B, code_leaves && h[1] < 0, ambig, rec_mat_ptr<KP, Real>(rj, 3), dD);
+                    if (h[c] >= 0) apply_t<KP, SPT>(sq, D[c], dD);   // Q_r D_c
+                    else if (c == 0) down<KP, SPT>(A, code_leaves, ambig, rec_mat_ptr<KP, Real>(rj, 1), dD);
+                    else down<KP, SPT>(B, code_leaves, ambig, rec_mat_ptr<KP, Real>(rj, 3), dD);
                     Real g = Real(0);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {

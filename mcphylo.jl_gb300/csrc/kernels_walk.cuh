@@ -1,8 +1,8 @@
 // Tree walk for the common case: every leaf operand is a table-row code (no dense
-// leaf values, no partially ambiguous codes).  Same work items, records, staging,
-// scratch layout and arithmetic as prune_kernel (kernels.cuh), operation for
-// operation, so the two give the same bits; written so that no operand is copied
-// between register arrays:
+// leaf values, no partially ambiguous codes).  Same work items, records, staging
+// and scratch layout as prune_kernel (kernels.cuh), and the same arithmetic
+// operation for operation (both keep Down vectors in the post-order column, below);
+// written so that no operand is copied between register arrays:
 //   - a leaf operand is its row codes (one uint32 per site), looked up straight
 //     into the Down vector; an internal operand 1 is the previous step's partial,
 //     P_1 is applied to it where it lies and the product is written back in place;
@@ -12,6 +12,10 @@
 //     is written where the next step reads it;
 //   - smaller staging chunks (at most 3 KB of records per buffer) so that more warps
 //     fit an SM.
+// The post-order column holds, for every internal non-root node, its Down vector
+// D = P L (the product its parent's step forms) rather than its partial L: the
+// gradient sweep reads D back instead of recomputing it, and forms dP L as Q_r D
+// (dP/dt = Q_r P, Q_r = U diag(D r mu) Uinv the scaled rate matrix of category r).
 // (FelsensteinFunction, src/Likelihood/LikelihoodCalculator_Node.jl:3-114;
 // comb_sum_product_loop!, by_max!, bymax!, root_sum, turbo_mul!, mygemmturbo!:
 // src/Likelihood/VectorizedFunctions.jl:2-213.)
@@ -34,10 +38,13 @@ __host__ __device__ constexpr int walk_chunk_steps(int kp, int real_bytes, int r
            : rpw * rec_bytes(kp, real_bytes) > 192  ? 8
                                                     : 16;
 }
+// per warp: two chunk buffers of records and of leaf codes, the stack slots, the
+// transposed scaled rate matrices Q_r^T of its categories, two mbarriers
 __host__ __device__ constexpr int walk_warp_smem_bytes(int kp, int spt, int real_bytes, int rpw = 1) {
     return (2 * walk_chunk_steps(kp, real_bytes, rpw) *
                 (rpw * rec_bytes(kp, real_bytes) + tip_bytes(kp, spt / rpw)) +
-            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) + 16 + 127) /
+            stack_smem_slots(kp, spt, real_bytes) * vec_bytes(kp, spt, real_bytes) +
+            rpw * kp * kp * real_bytes + 16 + 127) /
            128 * 128;
 }
 
@@ -129,8 +136,8 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
 
     unsigned char* wbase = smem + size_t(wib) * walk_warp_smem_bytes(KP, SPT, int(sizeof(Real)), RPW);
     Real* sstack = reinterpret_cast<Real*>(wbase + 2 * CH * (St::BYTES + St::TIP));
-    uint64_t* bars = reinterpret_cast<uint64_t*>(wbase + 2 * CH * (St::BYTES + St::TIP) +
-                                                  NS * SLOT * sizeof(Real));
+    Real* sq = sstack + NS * SLOT;              // Q_r^T of the warp's categories, KP x KP each
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sq + RPW * KP * KP);
     St st;
     st.init(wbase, bars, lane, a.wait_limit, a.inject_timeout != 0);
     if (lane == 0) fence_mbar_init();
@@ -152,6 +159,23 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
     auto mat_t = [&](const unsigned char* rj, int which, const Real (&x)[SPT][KP], Real (&y)[SPT][KP]) {
         if constexpr (RPW == 1) apply_tt<KP, SPT>(rec_mat_ptr<KP, Real>(rj, which), x, y);
         else apply_tt_q<KP, SPT, SPS>(rj, RB, which, x, y);
+    };
+    // dD = Q_r D for the warp's slots (dP/dt = Q_r P: a gradient term's dP L from the
+    // stored Down vector D = P L)
+    auto qmat = [&](const Real (&D)[SPT][KP], Real (&dD)[SPT][KP]) {
+        if constexpr (RPW == 1) {
+            apply_t<KP, SPT>(sq, D, dD);
+        } else {
+#pragma unroll
+            for (int u = 0; u < SPT; ++u) {
+                Real Du[1][KP], dDu[1][KP];
+#pragma unroll
+                for (int k = 0; k < KP; ++k) Du[0][k] = D[u][k];
+                apply_t<KP, 1>(sq + (u / SPS) * KP * KP, Du, dDu);
+#pragma unroll
+                for (int k = 0; k < KP; ++k) dD[u][k] = dDu[0][k];
+            }
+        }
     };
 
     for (;;) {
@@ -181,6 +205,16 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                   size_t(blk) * size_t(J) * St::TIP;
         st.J = J;
         st.Q = (J + CH - 1) / CH;
+        if (a.want_grad) {
+            // Q_r^T of the item's categories: sq[q][k][s] = Q_{r+q}[s][k], zero padded
+            const double* Qp = a.params + d.param_off + param_q_off(a.K, KP, C);
+            for (int e = lane; e < RPW * KP * KP; e += 32) {
+                const int q = e / (KP * KP), k = (e / KP) % KP, s2 = e % KP;
+                sq[e] = (s2 < a.K && k < a.K)
+                            ? Real(__ldg(Qp + int64_t(r * RPW + q) * a.K * a.K + s2 + a.K * k))
+                            : Real(0);
+            }
+        }
         __syncwarp();
         st.issue(0, lane);
         if (st.Q > 1) st.issue(1, lane);
@@ -196,11 +230,14 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
             const unsigned char* rj = st.rec(j);
             int h[8];
             rec_header(rj, h);
+            // the post-order column keeps, for every internal child, its Down vector
+            // D_c = P_c L_c (read back by the gradient sweep instead of recomputed)
             Real D0[SPT][KP];
             if (h[0] >= 0) {
                 Real A[SPT][KP];
                 read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
                 mat(rj, 0, A, D0);
+                if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, D0);
             } else {
                 uint32_t c[SPS];
                 read_rows<KP, SPS>(st.tip(j, 0), lane, c);
@@ -210,6 +247,7 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 Real D1[SPT][KP];
                 if (h[1] >= 0) {
                     mat(rj, 2, Lp, D1);
+                    if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, D1);
                 } else {
                     uint32_t c[SPS];
                     read_rows<KP, SPS>(st.tip(j, 1), lane, c);
@@ -219,8 +257,6 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
             }
             rescale_warp<KP, Real, SPT>(Lp, eacc);
             if (j + 1 < J) {
-                // the post-order column is only read back by the gradient sweep
-                if (a.want_grad) write_vec<KP, SPT>(post + int64_t(j) * SLOT, lane, Lp);
                 if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Lp);
             } else {
 #pragma unroll
@@ -266,9 +302,10 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
             }
         }
 
-        // One pre-order step j with header h: its internal operands are in X0 / X1
-        // (loaded one step ahead); loads step j-1's into Y0 / Y1 and its header into
-        // hn.  False when a staging wait gave up.
+        // One pre-order step j with header h: the Down vectors of its internal children
+        // are in X0 / X1 (loaded one step ahead; leaf children's are looked up into
+        // them); loads step j-1's into Y0 / Y1 and its header into hn.  False when a
+        // staging wait gave up.
         auto pstep = [&](int j, const int (&h)[8], int (&hn)[8], Real (&X0)[SPT][KP], Real (&X1)[SPT][KP],
                          Real (&Y0)[SPT][KP], Real (&Y1)[SPT][KP]) -> bool {
             const unsigned char* rj = st.rec(j);
@@ -292,11 +329,10 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, Y0);
                 if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, Y1);
             }
-            Real D0[SPT][KP], D1[SPT][KP];
-            if (h[0] >= 0) mat(rj, 0, X0, D0);
-            else look(rj, 0, c0, D0);
-            if (h[1] >= 0) mat(rj, 2, X1, D1);
-            else look(rj, 2, c1, D1);
+            if (h[0] < 0) look(rj, 0, c0, X0);
+            if (h[1] < 0) look(rj, 2, c1, X1);
+            Real (&D0)[SPT][KP] = X0;
+            Real (&D1)[SPT][KP] = X1;
             Real gsum[2] = {Real(0), Real(0)};   // this lane's gradient terms per child
             // wide state spaces: the gradient ratio's denominator pt_c . D_c =
             // sum_k pb_k D0_k D1_k is the same for both children, computed once
@@ -322,7 +358,7 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 }
                 if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
                     Real dD[SPT][KP];
-                    if (h[c] >= 0) mat(rj, 2 * c + 1, c == 0 ? X0 : X1, dD);
+                    if (h[c] >= 0) qmat(c == 0 ? D0 : D1, dD);
                     else look(rj, 2 * c + 1, c == 0 ? c0 : c1, dD);
                     Real g = Real(0);
 #pragma unroll

@@ -72,14 +72,19 @@ int build_level_plan(const SchedNode* nodes, int32_t J, int32_t* plan);
 
 // FP64 model parameters of one instance, packed at param_off:
 //   U (K*K, column-major) | D (K) | Uinv (K*K) | mu (1) | rates (C) | pi (Kp) |
-//   M = U * Uinv (K*K, column-major, each entry the exact sum rounded once)
+//   M = U * Uinv (K*K, column-major, each entry the exact sum rounded once) |
+//   Q_r = U diag(D rate_r mu) Uinv for r = 0..C-1 (K*K each, column-major): the
+//   scaled rate matrix, dP(t)/dt = Q_r P(t)
 #ifdef __CUDACC__
 #define MCPHY_HOST_DEVICE __host__ __device__
 #else
 #define MCPHY_HOST_DEVICE
 #endif
-inline MCPHY_HOST_DEVICE int64_t param_size(int K, int Kp, int C) { return 3 * K * K + K + 1 + C + Kp; }
+inline MCPHY_HOST_DEVICE int64_t param_size(int K, int Kp, int C) {
+    return 3 * K * K + K + 1 + C + Kp + int64_t(C) * K * K;
+}
 inline MCPHY_HOST_DEVICE int64_t param_m_off(int K, int Kp, int C) { return 2 * K * K + K + 1 + C + Kp; }
+inline MCPHY_HOST_DEVICE int64_t param_q_off(int K, int Kp, int C) { return 3 * K * K + K + 1 + C + Kp; }
 
 enum DirtyBits : unsigned {
     DIRTY_LAYOUT = 1u,   // schedule/offsets/buffer sizes changed
