@@ -1089,7 +1089,7 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
         for (int m = 0; m < K; ++m) {
             const double x = mu * t * Dv[m] * rate;
             em[m] = expm1(x);
-            de[m] = Dv[m] * rate * mu * exp(x);
+            de[m] = Dv[m] * rate * mu * (1.0 + em[m]);   // exp(x), one transcendental
         }
     for (int s = s0; s < Kp; s += R) {
         double rs = 0.0, drs = 0.0;

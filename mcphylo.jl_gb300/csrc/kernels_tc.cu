@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(128) build_records_tc_kernel(const BuildRecArg
         for (int m = 0; m < K; ++m) {
             const double x = mu * t * Dv[m] * rate;
             em[m] = expm1(x);
-            de[m] = Dv[m] * rate * mu * exp(x);
+            de[m] = Dv[m] * rate * mu * (1.0 + em[m]);   // exp(x), one transcendental
         }
     }
     double row = 0.0, drow = 0.0;

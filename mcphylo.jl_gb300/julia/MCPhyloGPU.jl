@@ -6,7 +6,7 @@ Julia binding of libmcphylo_gpu.so for MCPhylo.jl: `GPUPhyloDist` wraps a
 
     using MCPhylo, MCPhyloGPU
     pd  = PhyloDist(tree, pden, [1.0], [1.0], JC)
-    gpd = GPUPhyloDist(pd; precision = :f32)      # or :f64 (plain FP64), :tf32 / :bf16 (K >= 9)
+    gpd = GPUPhyloDist(pd; precision = :f32)      # or :f64 (plain FP64), :tf32 / :bf16 / :tf32x3 (K >= 9)
     logpdf(gpd, df); gradlogpdf(gpd, df)          # same results and layouts as pd
 
 In a model, use `GPUPhyloDist(PhyloDist(...))` where the reference uses
@@ -36,7 +36,7 @@ function check(st::Integer, h::Ptr{Cvoid})
     error("libmcphylo_gpu: $msg (status $st)")
 end
 
-const PRECISIONS = Dict(:f32 => 0, :f64 => 1, :tf32 => 2, :bf16 => 3)
+const PRECISIONS = Dict(:f32 => 0, :f64 => 1, :tf32 => 2, :bf16 => 3, :tf32x3 => 4)
 
 function Handle(nbase::Int, nrates::Int, precision::Symbol)
     haskey(PRECISIONS, precision) ||
