@@ -20,9 +20,11 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "mcphylo_gb300", "libmcphylo_gpu.so")
 SOURCES = ["schedule.cpp", "api.cu", "noalloc.cu", "kernels_common.cu", "kernels_f32.cu",
-           "kernels_f64.cu", "kernels_tc.cu", "kernels_level.cu", "tc_selftest.cu"]
+           "kernels_f32_g20.cu", "kernels_f32_g32.cu", "kernels_f32_narrow.cu", "kernels_f32_wide.cu", "kernels_f64.cu",
+           "kernels_f64_g20.cu", "kernels_f64_g32.cu", "kernels_f64_rnarrow.cu", "kernels_f64_rwide.cu", "kernels_tc.cu",
+           "kernels_level.cu", "tc_selftest.cu"]
 HEADERS = ["mcphy_internal.h", "kernels.cuh", "engine_state.h", "tc.cuh", "launch_attr.h",
-           "prune_launch.cuh", "kernels_walk.cuh"]
+           "prune_launch.cuh", "kernels_walk.cuh", "walk_subsets.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

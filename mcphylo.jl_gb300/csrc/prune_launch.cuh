@@ -18,7 +18,15 @@ __host__ __device__ constexpr int walk_spt_max(int kp, int real_bytes) {
     return real_bytes == 8 ? (kp <= 4 ? 2 : 1) : kp <= 4 ? 4 : kp == 8 ? 2 : 1;
 }
 
-template <typename Real>
+// Tree-walk kernels of one precision: the general one (any leaves) and the
+// row-code one (every leaf a table-row code).  Subset selects the shapes one
+// translation unit instantiates (the rest return cudaErrorNotSupported), so that the
+// instantiations compile in parallel: Subset::template want<KP, SPT, ROWS, RPW>().
+struct AllShapes {
+    template <int KP, int SPT, bool ROWS, int RPW>
+    static constexpr bool want() { return true; }
+};
+template <typename Real, typename Subset = AllShapes>
 struct PruneLaunch {
     template <int KP, int SPT, bool ROWS, int RPW>
     static const void* kernel() {
@@ -107,16 +115,20 @@ struct PruneLaunch {
                               cudaStream_t st) {
         return dispatch(Kp, spt, [&](auto kp, auto s) {
             return by_rpw<decltype(kp)::value, decltype(s)::value>(rows, rpw, [&](auto k2, auto s2, auto r2, auto q2) {
-                return go<decltype(k2)::value, decltype(s2)::value, decltype(r2)::value, decltype(q2)::value>(
-                    blocks, tpb, a, st);
+                constexpr int K_ = decltype(k2)::value, S_ = decltype(s2)::value, Q_ = decltype(q2)::value;
+                constexpr bool R_ = decltype(r2)::value;
+                if constexpr (Subset::template want<K_, S_, R_, Q_>()) return go<K_, S_, R_, Q_>(blocks, tpb, a, st);
+                else return cudaErrorNotSupported;
             });
         });
     }
     static cudaError_t occupancy(int Kp, int spt, int tpb, bool rows, int rpw, int* bps) {
         return dispatch(Kp, spt, [&](auto kp, auto s) {
             return by_rpw<decltype(kp)::value, decltype(s)::value>(rows, rpw, [&](auto k2, auto s2, auto r2, auto q2) {
-                return occ<decltype(k2)::value, decltype(s2)::value, decltype(r2)::value, decltype(q2)::value>(
-                    tpb, bps);
+                constexpr int K_ = decltype(k2)::value, S_ = decltype(s2)::value, Q_ = decltype(q2)::value;
+                constexpr bool R_ = decltype(r2)::value;
+                if constexpr (Subset::template want<K_, S_, R_, Q_>()) return occ<K_, S_, R_, Q_>(tpb, bps);
+                else return cudaErrorNotSupported;
             });
         });
     }
