@@ -650,7 +650,8 @@ def run_gpu(args, rank, world):
         kname = "prune_level_kernel<%d,float>" % kp
     else:
         alg = algorithmic_bytes(insts, tiles[0], real_b, args.mode == "grad")
-        kname = "prune_kernel<%d,float,%d>" % (kp, tiles[0])
+        # the benchmark workloads' leaves are all table-row codes: the row-code walk
+        kname = "prune_rows_kernel<%d,float,%d>" % (kp, tiles[0])
     pr = statistics.mean(prune_ms)
     achieved = alg / (pr / 1e3) / 1e9
     # DRAM bytes of one prune launch from the committed ncu capture: bytes per unit
