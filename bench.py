@@ -460,7 +460,7 @@ def run_gpu(args, rank, world):
     tc_path = prec in ("tf32", "bf16", "tf32x3")
     if tc_path and insts[0].K < 9:
         raise SystemExit("--precision tf32/bf16/tf32x3 is the dense-state path (K >= 9)")
-    if args.tiles == "auto" and args.sweep == "auto":
+    if args.tiles == "auto" and args.sweep == "auto" and args.walk == "auto" and not args.rates_per_warp:
         # the library's autotuner: times each sweep and launch shape on this problem
         e = make_engine(insts, prec)
         tiles = e.autotune()
@@ -469,8 +469,13 @@ def run_gpu(args, rank, world):
         tiles = None if args.tiles == "auto" else tuple(int(x) for x in args.tiles.split("x"))
         tune = {"chosen_by": "command line"}
         e = make_engine(insts, prec, tiles, args.sweep)
+        if args.rates_per_warp:
+            e.set_rates_per_warp(args.rates_per_warp)
+        if args.walk == "general":
+            e.debug_inject(3)   # the general tree walk (dense / ambiguous leaves) on every instance
         tiles = tiles or (1, 128)
     sweep = e.sweep() if not tc_path else "tensor-core"
+    rpw = e.tiles()[2] if not tc_path else 1
     M = len(insts)
     off = e.grad_offsets()
     G = int(off[-1])
@@ -651,7 +656,9 @@ def run_gpu(args, rank, world):
     else:
         alg = algorithmic_bytes(insts, tiles[0], real_b, args.mode == "grad")
         # the benchmark workloads' leaves are all table-row codes: the row-code walk
-        kname = "prune_rows_kernel<%d,float,%d>" % (kp, tiles[0])
+        # unless the general one is asked for
+        kname = ("prune_kernel<%d,float,%d>" % (kp, tiles[0]) if args.walk == "general" else
+                 "prune_rows_kernel<%d,float,%d%s>" % (kp, tiles[0], ",%d" % rpw if rpw > 1 else ""))
     pr = statistics.mean(prune_ms)
     achieved = alg / (pr / 1e3) / 1e9
     # DRAM bytes of one prune launch from the committed ncu capture: bytes per unit
@@ -700,7 +707,8 @@ def run_gpu(args, rank, world):
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": prec,
            "data": "synthetic (seeded simulation down Yule trees)",
-           "config": dict(cfg, tiles={"sites_per_thread": tiles[0], "threads_per_block": tiles[1]},
+           "config": dict(cfg, tiles={"sites_per_thread": tiles[0], "threads_per_block": tiles[1],
+                                      "rates_per_warp": rpw},
                           sweep=sweep,
                           l2="flushed between steps (512 MB write, outside the timed events)",
                           parallelism="replicas" if world > 1 else "single GPU"),
@@ -727,6 +735,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-hky-g4")
     ap.add_argument("--tiles", default="auto", help="auto or SPTxTPB, e.g. 2x256")
+    ap.add_argument("--walk", default="auto", choices=["auto", "general"],
+                    help="general: run the general tree-walk kernel instead of the row-code one")
+    ap.add_argument("--rates-per-warp", type=int, default=0, choices=[0, 1, 2, 4],
+                    help="rate categories per warp of the FP32 tree walk (0: the autotuner's)")
     ap.add_argument("--sweep", default="auto", choices=["auto", "walk", "level"],
                     help="SIMT sweep; auto with --tiles auto runs the library's autotuner")
     ap.add_argument("--mode", default="grad", choices=["grad", "logl", "nuts"],

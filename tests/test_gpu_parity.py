@@ -717,3 +717,37 @@ def test_injected_allocation_failure_is_reported_and_recoverable(built_lib):
     llo, go = oracle(bigger)
     assert abs(ll1 - llo) <= F32_LL_RTOL * abs(llo)
     assert_grad_close(g1, go, F32_G_RTOL, F32_G_FLOOR)
+
+
+def test_two_engines_on_two_host_threads(built_lib):
+    """Two handles evaluated concurrently from two host threads on one device (the
+    launch-attribute records are per device and behind a mutex; each handle has its
+    own stream and buffers): every result equals the same handle's result when run
+    alone, bit for bit."""
+    import threading
+    insts = [random_instance(4, 4, 80, 5000, seed=101), random_instance(2, 4, 120, 3000, seed=102,
+                                                                          model="restriction")]
+    engines = [engine(inst, "f32") for inst in insts]
+    alone = [e.logpdf_grad() for e in engines]
+    out = [[], []]
+    errors = []
+
+    def work(k):
+        try:
+            for _ in range(20):
+                out[k].append(engines[k].logpdf_grad())
+        except Exception as exc:   # reported below, in the main thread
+            errors.append(exc)
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for e in engines:
+        e.close()
+    assert not errors, errors
+    for k in range(2):
+        assert len(out[k]) == 20
+        for ll, g in out[k]:
+            assert ll == alone[k][0] and np.array_equal(g, alone[k][1])
