@@ -43,13 +43,15 @@ UNIT = "site-node updates/s"
 
 
 # ----------------------------------------------------------------------------- workloads
-def make_workload(name, workers):
+def make_workload(name, workers, site_scale=1.0):
     from mcphylo_gb300 import simulate
     if name == "batched-hky-g4":
-        insts = simulate.hky_batch(seed=4, n=256, workers=workers)
+        insts = simulate.hky_batch(seed=4, n=256, workers=workers, scale=site_scale)
         cfg = {"workload": "batched-hky-g4", "instances": 256, "taxa": "logU[16,1024]",
                "sites": "logU[500,50000]", "model": "HKY+G4 (shape 0.5), kappa~LogNormal(1,0.5)",
                "states": 4, "rates": 4}
+        if site_scale != 1.0:
+            cfg["site_scale"] = site_scale   # a profiling case, not the benchmark
     elif name == "gtr-g4":
         insts = [simulate.gtr_gamma(S=100_000, with_weights=True)]
         cfg = {"workload": "gtr-g4", "taxa": 128, "sites": "100,000 patterns",
@@ -446,7 +448,8 @@ def run_gpu(args, rank, world):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", rank=rank, world_size=world)
-    insts, cfg = make_workload(args.workload, workers=min(16, os.cpu_count() or 1))
+    insts, cfg = make_workload(args.workload, workers=min(16, os.cpu_count() or 1),
+                               site_scale=args.site_scale)
     units = cfg["units_per_step"]
     peaks = {}
     try:
@@ -735,6 +738,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched-hky-g4")
     ap.add_argument("--tiles", default="auto", help="auto or SPTxTPB, e.g. 2x256")
+    ap.add_argument("--site-scale", type=float, default=1.0,
+                    help="batched workload only: scale every instance's site count (profiling "
+                         "cases that fit an ncu capture; the benchmark is 1.0)")
     ap.add_argument("--walk", default="auto", choices=["auto", "general"],
                     help="general: run the general tree-walk kernel instead of the row-code one")
     ap.add_argument("--rates-per-warp", type=int, default=0, choices=[0, 1, 2, 4],
