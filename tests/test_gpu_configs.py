@@ -19,7 +19,8 @@ configuration 4, whose shortest branches, t ~ 1e-5, leave the reference's P(t) =
 U diag(exp) U^-1 -- followed by the oracle -- with relative errors up to ~6e-9 in its
 off-diagonal entries: the oracle is 1.2e-10 of max|g| from an extended-precision
 evaluation on one of its instances, while the engine builds P(t) as
-I + U diag(expm1) U^-1 without that cancellation); FP32
+M + U diag(expm1) U^-1, M = U U^-1 rounded once from a double-double product, without
+that cancellation); FP32
 logL 1e-6 relative, gradient entries 1e-4 relative to max(|g_i|, 1e-2 max|g|), and
 1e-4 relative with no floor on every entry whose condition number is at most 1000.
 The condition number of entry i is sum_{site,rate} |term| / |g_i| (from the
