@@ -354,9 +354,12 @@ def run_nuts(args):
     # workload, 2000 on the 512-taxon birth-death one
     n_iter = args.nuts_iter or (2000 if args.workload == "restriction-g4-bd" else 1000)
     n_adapt = args.nuts_adapt
+    # --nuts-plus-forward: the variant whose plus end starts with direction +1 (not the
+    # reference's sampler), FP32 engine only, to measure what the quirk costs
+    variant = bool(args.nuts_plus_forward)
     res = {}
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        for prec in ("f32", "f64"):
+        for prec in (("f32",) if variant else ("f32", "f64")):
             post = P.engine_posterior(inst.parent, inst.blen, inst.codes, inst.leaf_nums,
                                       (inst.U, inst.D, inst.Uinv, inst.mu), inst.pi, inst.rates,
                                       prior, precision=prec)
@@ -374,7 +377,7 @@ def run_nuts(args):
 
             ch = P.run_chain(inst.parent, inst.blen, timed(post.logfgrad), timed(post.logf),
                              n_iter=n_iter, n_adapt=n_adapt, seed=args.nuts_seed,
-                             target=args.nuts_target)
+                             target=args.nuts_target, plus_end_forward=variant)
             res[prec] = _chain_summary(ch)
             res[prec]["set_tree_calls"] = post.n_set_tree
             # host time of the sampling iterations: wall time minus the evaluations
@@ -395,6 +398,17 @@ def run_nuts(args):
             res[prec]["device_ms_per_grad_eval"] = statistics.median(dev[5:])
             res[prec]["launches_per_eval"] = e.counts()["launches"]
     clocks = clk.summary()
+    if variant:
+        out = {"metric": "NUTS ESS/s (PNUTS over branch lengths)", "value": res["f32"]["ess_per_s"],
+               "unit": "effective samples/s", "n_gpus": 1, "higher_is_better": True,
+               "dtype": "f32", "data": "synthetic (seeded simulation)",
+               "variant": "plus end starts with direction +1 (not the reference's sampler)",
+               "config": dict(cfg, iterations=n_iter, adaptation=n_adapt,
+                              prior="CompoundDirichlet(1,1,0.1,1)", target=args.nuts_target,
+                              tree_depth=10, seed=args.nuts_seed),
+               "nuts": {"f32": res["f32"]}, "clocks": clocks}
+        print(json.dumps(out), flush=True)
+        return 0
     # CPU: the oracle drives the same sampler.  With the same seed its chain retraces
     # the FP64 engine's (the decisions agree), so where a full run does not fit the
     # time budget, its time is the FP64 chain's evaluation counts at the oracle's
@@ -755,6 +769,9 @@ def main():
     ap.add_argument("--nuts-adapt", type=int, default=200)
     ap.add_argument("--nuts-seed", type=int, default=1)
     ap.add_argument("--nuts-target", type=float, default=0.8)
+    ap.add_argument("--nuts-plus-forward", action="store_true",
+                    help="non-parity sampler variant: the plus end of a trajectory starts "
+                         "with direction +1 (the reference starts both ends with -1)")
     ap.add_argument("--precision", default="f32", choices=["f32", "tf32", "bf16", "tf32x3"],
                     help="f32: FP32-scaled SIMT path; tf32 / bf16 / tf32x3: tensor-core node "
                          "updates with TF32 / BF16 / split-TF32 operands (K >= 9)")

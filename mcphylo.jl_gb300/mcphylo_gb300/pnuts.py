@@ -387,11 +387,17 @@ class PNUTS:
     """PNUTS(params; target=0.6, tree_depth=10, targetNNI=0.5, delta=0.003,
     jitter=0.0) (pnuts.jl:4-94) over one tree.  `logfgrad(parent, blen) ->
     (logf, grad)` and `logf(parent, blen) -> logf` evaluate the log posterior.
-    `sample(adapt)` is one iteration of sample! (pnuts.jl:103-143)."""
+    `sample(adapt)` is one iteration of sample! (pnuts.jl:103-143).
+
+    `plus_end_forward=True` is a variant that is NOT the reference's behaviour: the
+    plus end of every trajectory starts with direction +1 instead of -1
+    (pnuts.jl:197-198 starts both ends with -1).  It exists to measure what that
+    quirk costs in mixing; parity runs leave it off."""
 
     def __init__(self, parent, blen, logfgrad: Callable, logf: Callable, *, target=0.6,
                  tree_depth=10, targetNNI=0.5, delta=0.003, jitter=0.0, epsilon=-math.inf,
-                 rng: Optional[np.random.Generator] = None, max_refractions=1_000_000):
+                 rng: Optional[np.random.Generator] = None, max_refractions=1_000_000,
+                 plus_end_forward: bool = False):
         if not 0.0 <= jitter <= 1.0:
             raise ValueError("jitter must lie in [0, 1]")
         self.parent = np.asarray(parent, dtype=np.int64).copy()
@@ -406,6 +412,7 @@ class PNUTS:
         self.epsilon = float(epsilon)
         self.rng = rng if rng is not None else np.random.default_rng()
         self.max_refractions = max_refractions
+        self.plus_end_forward = bool(plus_end_forward)
         # NUTSstepadapter(0, 0.0, 0.0, NUTS_StepParams(0.5, target, 0.05, 0.75, 10, targetNNI))
         self.m = 0
         self.s_bar = 0.0
@@ -432,7 +439,8 @@ class PNUTS:
     _STATE = ("parent", "blen", "tree_depth", "delta", "jitter_amt", "epsilon", "m", "s_bar",
               "x_bar", "mu_p", "delta_p", "gamma_p", "kappa_p", "t0_p", "delta_nni",
               "metro_acc_prob", "nni_stat", "adapt", "moves", "att_moves", "tree_depth_trace",
-              "acc_p_r", "lf", "n_grad_evals", "n_logf_evals", "max_refractions")
+              "acc_p_r", "lf", "n_grad_evals", "n_logf_evals", "max_refractions",
+              "plus_end_forward")
 
     def state(self) -> dict:
         """Everything needed to continue the chain: tree, step-size adapter, traces
@@ -450,6 +458,8 @@ class PNUTS:
         bg.state = state["rng"]
         s = cls(state["parent"], state["blen"], logfgrad, logf, rng=np.random.Generator(bg))
         for k in cls._STATE:
+            if k not in state:   # a state saved before the field existed
+                continue
             v = state[k]
             setattr(s, k, v.copy() if isinstance(v, (np.ndarray, list)) else v)
         return s
@@ -592,7 +602,7 @@ class PNUTS:
         if math.isnan(self.lf):
             self.lf = logf
         xminus = ExtState(s0, -1)
-        xplus = ExtState(s0, -1)
+        xplus = ExtState(s0, 1 if self.plus_end_forward else -1)
         lu = math.log(self.rng.random())
         logp0 = -xminus.hamiltonian()
         nni_acc = 0

@@ -335,3 +335,21 @@ def test_checkpoint_resume_continues_the_chain():
     np.testing.assert_array_equal(a.blen, b.blen)
     assert a.epsilon == b.epsilon and a.tree_depth_trace == b.tree_depth_trace
     assert a.n_grad_evals == b.n_grad_evals
+
+
+def test_plus_end_forward_variant():
+    """The non-parity variant (plus end starts with direction +1) still samples the
+    target; the default keeps the reference's -1 for both ends, so the two chains
+    differ from the first trajectory on."""
+    tree = yule_tree(8, np.random.default_rng(0), 0.1)
+    parent, blen = to_parent(tree)
+    runs = {}
+    for fwd in (False, True):
+        runs[fwd] = P.run_chain(parent, np.full(len(blen), 1.0), _gamma_target,
+                                lambda p, b: _gamma_target(p, b)[0], n_iter=1500, n_adapt=300,
+                                seed=3, target=0.8, plus_end_forward=fwd)
+    assert abs(runs[True].blen.mean() - SHAPE * SCALE) < 0.03
+    assert not np.array_equal(runs[True].blen, runs[False].blen)
+    s = _sampler(parent, blen, _gamma_target)
+    assert s.plus_end_forward is False
+    assert P.PNUTS.from_state(s.state(), _gamma_target, _flat).plus_end_forward is False
