@@ -209,42 +209,48 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- CPU sample
-def cpu_sample(insts, seconds, window=2000):
-    """The oracle (FP64 restatement of the reference loops, OpenMP over all host
-    cores) on the workload itself: instance by instance, window of ``window``
-    sites by window, until ``seconds`` of oracle time have been spent.  Only the
-    oracle's logL + gradient call is timed."""
+def oracle_windows(insts, units_budget, window=2000):
+    """The bounded CPU sample of a workload, the same for the reference arm and the
+    cpu_baseline leg: windows of at most ``window`` sites, one per instance, the
+    instances taken at a fixed stride through the workload (so a batched workload's
+    sample spans its range of tree and alignment sizes), until ``units_budget``
+    units; a single-instance workload gives consecutive windows of its sites.
+    Returns [(oracle tree, site tensor, instance window)]."""
     from oracle import pyoracle as O
     from mcphylo_gb300 import simulate
-    O.lib()
-    units = 0
-    calls = 0
-    spent = 0.0
-    insts_used = set()
-    done = False
-    while not done:
-        for ii, b in enumerate(insts):
-            for s0 in range(0, b.S, window):
-                sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums,
-                                        b.codes[:, s0:s0 + window], b.U, b.D, b.Uinv, b.mu,
-                                        b.pi, b.rates)
-                x = sub.tensor()
-                t = O.tree_from_parent(sub.parent, sub.blen)
-                ts = time.perf_counter()
-                O.gradlogpdf(t, x, sub.pi, (sub.U, sub.D, sub.Uinv, sub.mu), sub.rates)
-                spent += time.perf_counter() - ts
-                units += sub.units()
-                calls += 1
-                insts_used.add(ii)
-                if spent >= seconds:
-                    done = True
-                    break
-                if len(insts) > 1:
-                    break          # batched workload: one window per instance, spread out
-            if done:
-                break
-    return units / spent, {"instances": len(insts_used), "window": window, "calls": calls,
-                           "units": units, "seconds": round(spent, 3), "threads": O.num_threads()}
+    n = len(insts)
+    stride = 97 if n > 97 and n % 97 else 1
+    order = [(i * stride) % n for i in range(n)]
+    out, units = [], 0
+    rounds = 1 if n > 1 else max(1, -(-insts[0].S // window))
+    for r in range(rounds):
+        for ii in order:
+            b = insts[ii]
+            s0 = r * window
+            sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums,
+                                    b.codes[:, s0:s0 + window], b.U, b.D, b.Uinv, b.mu,
+                                    b.pi, b.rates)
+            out.append((O.tree_from_parent(sub.parent, sub.blen), sub.tensor(), sub))
+            units += sub.units()
+            if units >= units_budget:
+                return out
+    return out
+
+
+def cpu_leg(args):
+    """The cpu_baseline leg of the GPU arm: the reference arm (the oracle on its
+    bounded sample, oracle_windows) run as a child process, so that it times the same
+    code on the same windows in a process whose cores no GPU-side runtime (torch's
+    thread pool, the clock sampler) shares.  Returns the reference arm's JSON line."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload",
+           args.workload, "--steps", str(args.cpu_steps), "--warmup", "3", "--ref-units",
+           str(args.ref_units)]
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    p = subprocess.run(cmd, capture_output=True, text=True, env=env,
+                       cwd=os.path.dirname(os.path.abspath(__file__)))
+    if p.returncode != 0:
+        raise RuntimeError("cpu_baseline leg failed: " + p.stderr[-2000:])
+    return json.loads(p.stdout.strip().splitlines()[-1])
 
 
 # ----------------------------------------------------------------------------- reference arm
@@ -253,19 +259,10 @@ def run_reference(args, rank, world):
         return 0
     insts, cfg = make_workload(args.workload, workers=min(16, os.cpu_count() or 1))
     from oracle import pyoracle as O
-    from mcphylo_gb300 import simulate
     O.lib()
-    # one step = the oracle's logL + gradient on a fixed bounded sample
-    sample = []
-    budget = args.ref_units
-    for b in insts:
-        S = min(b.S, 2000)
-        sub = simulate.Instance(b.tree, b.parent, b.blen, b.leaf_nums, b.codes[:, :S], b.U, b.D,
-                                b.Uinv, b.mu, b.pi, b.rates)
-        sample.append((O.tree_from_parent(sub.parent, sub.blen), sub.tensor(), sub))
-        budget -= sub.units()
-        if budget <= 0:
-            break
+    # one step = the oracle's logL + gradient on a fixed bounded sample (the same
+    # windows as the cpu_baseline leg of the GPU arm)
+    sample = oracle_windows(insts, args.ref_units)
     units = sum(s[2].units() for s in sample)
 
     def step():
@@ -281,8 +278,8 @@ def run_reference(args, rank, world):
         times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.mean(times)
     v = units / (ms / 1e3)
-    desc = (f"{len(sample)} of the workload's instances, first <=2000 sites each, "
-            f"{units} units per step")
+    desc = (f"{len(sample)} windows of <=2000 sites (one per instance, instances at a fixed "
+            f"stride through the workload), {units} units per step")
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -712,11 +709,11 @@ def run_gpu(args, rank, world):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, info = cpu_sample(insts, args.cpu_seconds)
-        cpu = {"value": v, "unit": UNIT, "cores": info["threads"], "kind": "port",
-               "sample": f"oracle (FP64, OpenMP) on {info['calls']} windows of <={info['window']} "
-                         f"sites from {info['instances']} of the workload's instances, "
-                         f"{info['units']} units in {info['seconds']} s of oracle time"}
+        ref = cpu_leg(args)
+        cpu = {"value": ref["value"], "unit": UNIT, "cores": ref["cpu_baseline"]["cores"],
+               "kind": "port",
+               "sample": "oracle (FP64, OpenMP) in a child process: the reference arm, "
+                         f"{args.cpu_steps} steps of {ref['cpu_baseline']['sample']}"}
 
     metric = METRIC if args.mode == "grad" else \
         "logL-only site-node updates/s, FP32-scaled vs plain FP64 GPU at ≤1e-6 rel err"
@@ -778,7 +775,10 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="oracle time of the NUTS mode's CPU estimate")
+    ap.add_argument("--cpu-steps", type=int, default=6,
+                    help="timed steps of the reference arm run as the cpu_baseline leg")
     ap.add_argument("--ref-units", type=float, default=6e7,
                     help="units per step of the reference arm's bounded sample")
     args = ap.parse_args()

@@ -454,6 +454,7 @@ struct Stage {
     static constexpr int BYTES = STEP_BYTES;
     static constexpr int TIP = TIP_BYTES;
     static constexpr int CH = CH_;
+    static_assert(CH > 0 && (CH & (CH - 1)) == 0, "chunks of a power of two steps");
     unsigned char* base;        // record buffer 0, record buffer 1, tip buffer 0, tip buffer 1
     uint64_t* bars;             // two mbarriers
     uint32_t parity;            // bit b: phase parity expected next on buffer b
@@ -509,13 +510,14 @@ struct Stage {
         ok = ok && done;
         return done;
     }
+    // (j >= 0; CH is a power of two, so buffer b and slot s of step j are the low
+    // bits of j: b * CH + s = j mod 2 CH)
     __device__ const unsigned char* rec(int j) const {
-        return base + ((j / CH) & 1) * (CH * BYTES) + (j % CH) * BYTES;
+        return base + (unsigned(j) % unsigned(2 * CH)) * BYTES;
     }
     // leaf codes of operand c of step j
     __device__ const unsigned char* tip(int j, int c) const {
-        return base + 2 * CH * BYTES + ((j / CH) & 1) * (CH * TIP) + (j % CH) * TIP +
-               c * (TIP / 2);
+        return base + 2 * CH * BYTES + (unsigned(j) % unsigned(2 * CH)) * TIP + c * (TIP / 2);
     }
 };
 

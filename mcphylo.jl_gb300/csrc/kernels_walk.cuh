@@ -119,6 +119,7 @@ __device__ __forceinline__ void vmul(Real (&L)[SPT][KP], const Real (&X)[SPT][KP
 template <int KP, typename Real, int SPT, int RPW = 1>
 __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
     static_assert(SPT % RPW == 0, "the vector slots hold whole groups of categories");
+    static_assert(walk_chunk_steps(KP, sizeof(Real), RPW) <= 16, "gradient entries wait in half a warp");
     constexpr int SPS = SPT / RPW;                  // sites per thread
     constexpr int RB = rec_bytes(KP, sizeof(Real)); // one category's record
     constexpr int CH = walk_chunk_steps(KP, sizeof(Real), RPW);
@@ -220,63 +221,68 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
         if (st.Q > 1) st.issue(1, lane);
 
         // ---------------- post-order sweep (logL)
+        // chunk by chunk: one wait before a chunk's steps, its buffers refilled (with
+        // the chunk after next) once its last step is done; record and leaf-code
+        // pointers advance by one step's bytes
         uint32_t eacc[SPT];
 #pragma unroll
         for (int u = 0; u < SPT; ++u) eacc[u] = 0u;
         double ll_lane = 0.0;
         Real Lp[SPT][KP];          // the previous step's partial (operand 1 of the next step)
-        for (int j = 0; j < J; ++j) {
-            if (j % CH == 0 && !st.wait(j / CH)) break;
-            const unsigned char* rj = st.rec(j);
-            int h[8];
-            rec_header(rj, h);
-            // the post-order column keeps, for every internal child, its Down vector
-            // D_c = P_c L_c (read back by the gradient sweep instead of recomputed)
-            Real D0[SPT][KP];
-            if (h[0] >= 0) {
-                Real A[SPT][KP];
-                read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
-                mat(rj, 0, A, D0);
-                if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, D0);
-            } else {
-                uint32_t c[SPS];
-                read_rows<KP, SPS>(st.tip(j, 0), lane, c);
-                look(rj, 0, c, D0);
-            }
-            {
-                Real D1[SPT][KP];
-                if (h[1] >= 0) {
-                    mat(rj, 2, Lp, D1);
-                    if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, D1);
+        for (int q = 0; q < st.Q; ++q) {
+            if (!st.wait(q)) break;
+            const unsigned char* rj = st.rec(q * CH);
+            const unsigned char* tj = st.tip(q * CH, 0);
+            const int jend = min(J, q * CH + CH);
+            for (int j = q * CH; j < jend; ++j, rj += St::BYTES, tj += St::TIP) {
+                int h[8];
+                rec_header(rj, h);
+                // the post-order column keeps, for every internal child, its Down vector
+                // D_c = P_c L_c (read back by the gradient sweep instead of recomputed)
+                Real D0[SPT][KP];
+                if (h[0] >= 0) {
+                    Real A[SPT][KP];
+                    read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
+                    mat(rj, 0, A, D0);
+                    if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, D0);
                 } else {
                     uint32_t c[SPS];
-                    read_rows<KP, SPS>(st.tip(j, 1), lane, c);
-                    look(rj, 2, c, D1);
+                    read_rows<KP, SPS>(tj, lane, c);
+                    look(rj, 0, c, D0);
                 }
-                vmul<KP, SPT>(Lp, D0, D1);
-            }
-            rescale_warp<KP, Real, SPT>(Lp, eacc);
-            if (j + 1 < J) {
-                if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Lp);
-            } else {
+                {
+                    Real D1[SPT][KP];
+                    if (h[1] >= 0) {
+                        mat(rj, 2, Lp, D1);
+                        if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, D1);
+                    } else {
+                        uint32_t c[SPS];
+                        read_rows<KP, SPS>(tj + St::TIP / 2, lane, c);
+                        look(rj, 2, c, D1);
+                    }
+                    vmul<KP, SPT>(Lp, D0, D1);
+                }
+                rescale_warp<KP, Real, SPT>(Lp, eacc);
+                if (j + 1 < J) {
+                    if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Lp);
+                } else {
 #pragma unroll
-                for (int u = 0; u < SPT; ++u) {
-                    Real lik = Real(0);
+                    for (int u = 0; u < SPT; ++u) {
+                        Real lik = Real(0);
 #pragma unroll
-                    for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Lp[u][k], lik);
-                    const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
-                    const double v = log_site(lik) + double(ex) * LN2;
-                    const int site = site0 + 32 * (u % SPS);
-                    const bool valid = site < d.S;
-                    const double w = valid ? __ldg(a.weights + d.weight_off + site) : 0.0;
-                    ll_lane += valid ? w * v : 0.0;
+                        for (int k = 0; k < KP; ++k) lik = fma(Real(__ldg(pi_d + k)), Lp[u][k], lik);
+                        const int ex = int(eacc[u]) - J * ExpBias<Real>::value;
+                        const double v = log_site(lik) + double(ex) * LN2;
+                        const int site = site0 + 32 * (u % SPS);
+                        const bool valid = site < d.S;
+                        const double w = valid ? __ldg(a.weights + d.weight_off + site) : 0.0;
+                        ll_lane += valid ? w * v : 0.0;
+                    }
                 }
             }
             // chunk finished: refill its buffers with the chunk after next
-            if ((j + 1) % CH == 0 || j + 1 == J) {
-                __syncwarp();
-                if (j / CH + 2 < st.Q) st.issue(j / CH + 2, lane);
-            }
+            __syncwarp();
+            if (q + 2 < st.Q) st.issue(q + 2, lane);
         }
         if (!st.ok) break;
         ll_lane = warp_sum(ll_lane);
@@ -292,40 +298,55 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
         for (int u = 0; u < SPT; ++u)
 #pragma unroll
             for (int k = 0; k < KP; ++k) pb[u][k] = Real(__ldg(pi_d + k));
-        if (lane == 0) {
-            // the first PF_DIST steps' post-order partials (later ones: from the records)
-            for (int q = 0; q < PF_DIST && q < CH && q < J; ++q) {
-                int hq[8];
-                rec_header(st.rec(J - 1 - q), hq);
-                for (int c = 0; c < 2; ++c)
-                    if (hq[c] >= 0) prefetch_l2(post + int64_t(hq[c]) * SLOT, SLOT * sizeof(Real));
-            }
-        }
+        // L2 prefetch of the post-order column, a chunk at a time (lane 0, when the
+        // chunk's records are in): the operands of the steps PF_DIST below the chunk's
+        // steps (the records' prefetch fields), so every step's Down vectors are
+        // requested at least PF_DIST steps ahead; at the start also the operands of
+        // the steps already staged
+        auto prefetch_chunk = [&](int lo, int hi, bool own) {
+            if (lane == 0)
+                for (int jj = lo; jj < hi; ++jj) {
+                    if (own) {
+                        int hq[8];
+                        rec_header(st.rec(jj), hq);
+                        if (hq[0] >= 0) prefetch_l2(post + int64_t(hq[0]) * SLOT, SLOT * sizeof(Real));
+                        if (hq[1] >= 0) prefetch_l2(post + int64_t(hq[1]) * SLOT, SLOT * sizeof(Real));
+                    }
+                    const int2 pf = rec_prefetch(st.rec(jj));
+                    if (pf.x >= 0) prefetch_l2(post + int64_t(pf.x) * SLOT, SLOT * sizeof(Real));
+                    if (pf.y >= 0) prefetch_l2(post + int64_t(pf.y) * SLOT, SLOT * sizeof(Real));
+                }
+        };
+        prefetch_chunk(low * CH, J, true);
+        // gradient entries of the chunk's steps wait in lanes until the chunk is done:
+        // step j's child-0 sum in lane j % CH, its child-1 sum in lane 16 + j % CH
+        // (CH <= 16), with the entry index beside it (-1: nothing to write)
+        Real gstash = Real(0);
+        int gidx = -1;
 
-        // One pre-order step j with header h: the Down vectors of its internal children
-        // are in X0 / X1 (loaded one step ahead; leaf children's are looked up into
-        // them); loads step j-1's into Y0 / Y1 and its header into hn.  False when a
-        // staging wait gave up.
-        auto pstep = [&](int j, const int (&h)[8], int (&hn)[8], Real (&X0)[SPT][KP], Real (&X1)[SPT][KP],
-                         Real (&Y0)[SPT][KP], Real (&Y1)[SPT][KP]) -> bool {
-            const unsigned char* rj = st.rec(j);
-            if (lane == 0) {
-                const int2 pf = rec_prefetch(rj);
-                if (pf.x >= 0) prefetch_l2(post + int64_t(pf.x) * SLOT, SLOT * sizeof(Real));
-                if (pf.y >= 0) prefetch_l2(post + int64_t(pf.y) * SLOT, SLOT * sizeof(Real));
-            }
+        // One pre-order step j with record rj and header h: the Down vectors of its
+        // internal children are in X0 / X1 (loaded one step ahead; leaf children's are
+        // looked up into them); loads step j-1's into Y0 / Y1, its record into rjn and
+        // its header into hn.  False when a staging wait gave up.
+        auto pstep = [&](int j, const unsigned char* rj, const int (&h)[8], const unsigned char*& rjn,
+                         int (&hn)[8], Real (&X0)[SPT][KP], Real (&X1)[SPT][KP], Real (&Y0)[SPT][KP],
+                         Real (&Y1)[SPT][KP]) -> bool {
+            const unsigned js = unsigned(j) % unsigned(CH);   // slot of step j in its chunk
             if (h[3] >= 0) read_vec<KP, SPT>(stack_ptr(h[3]), lane, pb);   // else carried
             uint32_t c0[SPS], c1[SPS];
-            if (h[0] < 0) read_rows<KP, SPS>(st.tip(j, 0), lane, c0);
-            if (h[1] < 0) read_rows<KP, SPS>(st.tip(j, 1), lane, c1);
+            const unsigned char* tj = st.tip(j, 0);
+            if (h[0] < 0) read_rows<KP, SPS>(tj, lane, c0);
+            if (h[1] < 0) read_rows<KP, SPS>(tj + St::TIP / 2, lane, c1);
             // operands of the next step, one step ahead
             if (j > 0) {
-                const int qn = (j - 1) / CH;
+                const int qn = int(unsigned(j - 1) / unsigned(CH));
                 if (qn < low) {
                     if (!st.wait(qn)) return false;
                     low = qn;
+                    prefetch_chunk(qn * CH, qn * CH + CH, false);
                 }
-                rec_header(st.rec(j - 1), hn);
+                rjn = st.rec(j - 1);
+                rec_header(rjn, hn);
                 if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, Y0);
                 if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, Y1);
             }
@@ -405,26 +426,34 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 v += __shfl_xor_sync(0xffffffffu, hi ? gsum[0] : gsum[1], 16);
 #pragma unroll
                 for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                if (lane == 0 && h[4] >= 0) pg[h[4]] = v;
-                if (lane == 16 && h[5] >= 0) pg[h[5]] = v;
+                if (unsigned(lane & 15) == js) {
+                    gstash = v;
+                    gidx = hi ? h[5] : h[4];
+                }
             }
-            // chunk finished (descending): refill its buffers two chunks below
-            if (j % CH == 0) {
+            // chunk finished (descending): its gradient entries out, its buffers
+            // refilled two chunks below
+            if (js == 0) {
+                if (gidx >= 0) pg[gidx] = gstash;
+                gidx = -1;
                 __syncwarp();
-                if (j / CH - 2 >= 0) st.issue(j / CH - 2, lane);
+                const int qj = int(unsigned(j) / unsigned(CH));
+                if (qj >= 2) st.issue(qj - 2, lane);
             }
             return true;
         };
 
         int h[8], hn[8];
-        rec_header(st.rec(J - 1), h);
+        const unsigned char* ra = st.rec(J - 1);
+        const unsigned char* rb = ra;
+        rec_header(ra, h);
         Real Xa[SPT][KP], Xb[SPT][KP], Ya[SPT][KP], Yb[SPT][KP];
         if (h[0] >= 0) read_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, Xa);
         if (h[1] >= 0) read_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, Xb);
         for (int j = J - 1; j >= 0;) {
-            if (!pstep(j, h, hn, Xa, Xb, Ya, Yb)) break;
+            if (!pstep(j, ra, h, rb, hn, Xa, Xb, Ya, Yb)) break;
             if (--j < 0) break;
-            if (!pstep(j, hn, h, Ya, Yb, Xa, Xb)) break;
+            if (!pstep(j, rb, hn, ra, h, Ya, Yb, Xa, Xb)) break;
             --j;
         }
         if (!st.ok) break;

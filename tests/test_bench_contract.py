@@ -5,6 +5,8 @@ import os
 import subprocess
 import sys
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ARGS = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
         "restriction", "--steps", "1", "--warmup", "3", "--ref-units", "2e5"]
@@ -37,3 +39,32 @@ def test_reference_arm_other_ranks_exit_quietly():
     p = _run({"RANK": "1", "WORLD_SIZE": "2"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+def test_cpu_legs_share_one_sample():
+    """The reference arm and the GPU arm's cpu_baseline time the oracle on the same
+    windows: one per instance, at a fixed stride through the workload, up to the
+    unit budget."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from mcphylo_gb300 import simulate
+    insts = [simulate.restriction_small(seed=s) for s in range(5)]
+    per = insts[0].units()
+    w = bench.oracle_windows(insts, 3 * per - 1)
+    assert len(w) == 3 and [x[2].parent is insts[i].parent for i, x in enumerate(w)] == [True] * 3
+    w2 = bench.oracle_windows(insts, 3 * per - 1)
+    assert all(np.array_equal(a[2].codes, b[2].codes) for a, b in zip(w, w2))
+    one = bench.oracle_windows([simulate.restriction_small()], 1e12, window=300)
+    assert len(one) == 4 and sum(x[2].codes.shape[1] for x in one) == 1000
+
+
+def test_gpu_arm_cpu_leg_is_the_reference_arm():
+    """The GPU arm's cpu_baseline leg runs the reference arm in a child process and
+    reports its line."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    a = argparse.Namespace(workload="restriction", cpu_steps=1, ref_units=2e5)
+    out = bench.cpu_leg(a)
+    assert out["impl"] == "reference" and out["steps"] == 1 and out["value"] > 0
+    assert out["config"]["workload"] == "restriction"
