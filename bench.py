@@ -50,27 +50,27 @@ def make_workload(name, workers, site_scale=1.0):
         cfg = {"workload": "batched-hky-g4", "instances": 256, "taxa": "logU[16,1024]",
                "sites": "logU[500,50000]", "model": "HKY+G4 (shape 0.5), kappa~LogNormal(1,0.5)",
                "states": 4, "rates": 4}
-        if site_scale != 1.0:
-            cfg["site_scale"] = site_scale   # a profiling case, not the benchmark
     elif name == "gtr-g4":
-        insts = [simulate.gtr_gamma(S=100_000, with_weights=True)]
+        insts = [simulate.gtr_gamma(S=max(1, int(100_000 * site_scale)), with_weights=True)]
         cfg = {"workload": "gtr-g4", "taxa": 128, "sites": "100,000 patterns",
                "pattern_weights": "Poisson(1)+1", "model": "GTR+G4 (shape 0.5)",
                "states": 4, "rates": 4}
     elif name == "restriction":
-        insts = [simulate.restriction_small()]
+        insts = [simulate.restriction_small(S=max(1, int(1000 * site_scale)))]
         cfg = {"workload": "restriction", "taxa": 32, "sites": 1000, "model": "Restriction",
                "states": 2, "rates": 1}
     elif name == "restriction-g4-bd":
-        insts = [simulate.restriction_gamma_bd()]
+        insts = [simulate.restriction_gamma_bd(S=max(1, int(20_000 * site_scale)))]
         cfg = {"workload": "restriction-g4-bd", "taxa": 512, "sites": 20_000,
                "model": "Restriction+G4 (shape 1)", "states": 2, "rates": 4}
     elif name == "protein-g4":
-        insts = [simulate.protein_gamma()]
+        insts = [simulate.protein_gamma(S=max(1, int(50_000 * site_scale)))]
         cfg = {"workload": "protein-g4", "taxa": 256, "sites": 50_000,
                "model": "GTR20+G4 (shape 0.5)", "states": 20, "rates": 4}
     else:
         raise SystemExit(f"unknown workload {name}")
+    if site_scale != 1.0:
+        cfg["site_scale"] = site_scale   # a profiling case, not the benchmark
     cfg["units_per_step"] = int(sum(i.units() for i in insts))
     return insts, cfg
 
@@ -750,8 +750,8 @@ def main():
     ap.add_argument("--workload", default="batched-hky-g4")
     ap.add_argument("--tiles", default="auto", help="auto or SPTxTPB, e.g. 2x256")
     ap.add_argument("--site-scale", type=float, default=1.0,
-                    help="batched workload only: scale every instance's site count (profiling "
-                         "cases that fit an ncu capture; the benchmark is 1.0)")
+                    help="scale every instance's site count (profiling cases that fit an ncu "
+                         "capture; the benchmark is 1.0)")
     ap.add_argument("--walk", default="auto", choices=["auto", "general"],
                     help="general: run the general tree-walk kernel instead of the row-code one")
     ap.add_argument("--rates-per-warp", type=int, default=0, choices=[0, 1, 2, 4],

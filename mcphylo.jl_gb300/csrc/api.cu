@@ -357,7 +357,15 @@ int layout(mcphy_engine* h) {
     if ((rc = ensure(h, h->d_pgrad, rs * size_t(pgrad_off)))) return rc;
     int64_t max_items = 0;
     for (const InstanceDesc& d : h->desc) max_items = std::max<int64_t>(max_items, int64_t(G) * d.n_blocks);
-    h->n_split = int(std::min<int64_t>(64, std::max<int64_t>(1, (max_items + 127) / 128)));
+    h->n_split = int(std::min<int64_t>(64, std::max<int64_t>(1, (max_items + RED_ITEMS - 1) / RED_ITEMS)));
+    // first-pass blocks of the reduction, instance by instance
+    int64_t red_blocks = 0;
+    for (InstanceDesc& d : h->desc) {
+        d.red_off = int32_t(red_blocks);
+        red_blocks += int64_t(red_splits(int64_t(G) * d.n_blocks, h->n_split)) * red_groups(d.n_branch);
+    }
+    if (red_blocks >= (int64_t(1) << 31)) return fail(h, MCPHY_ERR_ARG, "too many instances");
+    h->red_blocks = int32_t(red_blocks);
     if ((rc = ensure(h, h->d_part, sizeof(double) * size_t(h->n_split) *
                                        size_t(h->M + h->total_branch))))
         return rc;
@@ -767,6 +775,7 @@ int run(mcphy_engine* h, bool want_grad) {
     r.n_inst = int32_t(h->M);
     r.C = h->C / h->rpw;   // work items per site block
     r.n_split = h->n_split;
+    r.red_blocks = h->red_blocks;
     r.want_grad = want_grad ? 1 : 0;
     r.total_branch = h->total_branch;
     r.pgrad = a.pgrad;

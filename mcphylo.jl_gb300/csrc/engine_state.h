@@ -97,6 +97,7 @@ struct mcphy_engine {
         d_blen, d_pgrad, d_pll, d_part, d_out, d_post, d_pre, d_counter, d_leafcodes, d_weights,
         d_plan;
     int n_split = 1;
+    int32_t red_blocks = 1;   // first-pass blocks of the reduction
 
     double* h_blen = nullptr;
     size_t h_blen_cap = 0;

@@ -208,8 +208,9 @@ struct ReduceArgs {
     const InstanceDesc* inst;
     int32_t n_inst;
     int32_t C;
-    int32_t n_split;          // item ranges summed independently in the first pass
+    int32_t n_split;          // most item ranges of an instance (red_splits caps each at it)
     int32_t want_grad;
+    int32_t red_blocks;       // first-pass blocks: sum over instances of splits x groups
     int64_t total_branch;     // packed gradient length
     const void* pgrad;        // Real [item][branch]
     const double* pll;

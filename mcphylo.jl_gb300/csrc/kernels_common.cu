@@ -6,25 +6,38 @@
 namespace mcphy {
 
 // ---------------------------------------------------------------- reduction
-// Pass 1: grid (ceil(max_branch/32) + 1, n_inst, n_split), block (32, RY).
-// Block (bx, i, z) sums the items of instance i in split z (a contiguous item
-// range) for 32 branches; thread (tx, ty) takes every RY-th item of the range,
-// then the RY partial sums are added in ty order.  The last x-block does the
-// log-likelihood partials (a shuffle tree per warp, then the warp sums in order).
-// Pass 2 adds the n_split sums in z order; with one split, pass 1 writes the results.
+// Pass 1: one block (32, RY) per (instance i, split z, group g), z < red_splits(items
+// of i), g < red_groups(branches of i), in a 1D grid: instance i owns blocks
+// [red_off, red_off + splits x groups), split-major.  Split z is a contiguous range of
+// the instance's items.  Group g < groups - 1 sums that range for 32 branches: thread
+// (tx, ty) takes every RY-th item of the range, then the RY partial sums are added in
+// ty order.  The last group does the log-likelihood partials (a shuffle tree per warp,
+// then the warp sums in order).  Pass 2 adds an instance's splits in z order; when no
+// instance has more than one split, pass 1 writes the results.
 template <typename Real>
 __global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
     __shared__ double red[RY][33];
-    const int i = blockIdx.y;
+    // the instance of this block: the last one whose first block is not past it
+    const int blk = int(blockIdx.x);
+    int lo = 0, hi = a.n_inst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.inst[mid].red_off <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    const int i = lo;
     const InstanceDesc& d = a.inst[i];
     const int64_t n_items = int64_t(a.C) * d.n_blocks;
-    const int64_t per = (n_items + a.n_split - 1) / a.n_split;
-    const int64_t q0 = int64_t(blockIdx.z) * per;
+    const int Z = red_splits(n_items, a.n_split), G = red_groups(d.n_branch);
+    const int w = blk - d.red_off;
+    const int z = w / G, g = w - z * G;
+    const int64_t per = (n_items + Z - 1) / Z;
+    const int64_t q0 = int64_t(z) * per;
     const int64_t q1 = min(n_items, q0 + per);
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t stride = int64_t(a.total_branch) + gridDim.y;   // one split row
-    double* part = a.part + int64_t(blockIdx.z) * stride;
-    if (blockIdx.x == gridDim.x - 1) {
+    const int64_t stride = int64_t(a.total_branch) + a.n_inst;   // one split row
+    double* part = a.part + int64_t(z) * stride;
+    if (g == G - 1) {
         const int tid = ty * 32 + tx;
         double acc = 0.0;
         for (int64_t q = q0 + tid; q < q1; q += 32 * RY) acc += a.pll[d.item_off + q];
@@ -40,11 +53,12 @@ __global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
         return;
     }
     if (!a.want_grad) return;
-    const int b = blockIdx.x * 32 + tx;
-    if (blockIdx.x * 32 >= d.n_branch) return;      // whole block past this instance
+    const int b = g * 32 + tx;
     double acc = 0.0;
     if (b < d.n_branch) {
         const Real* pg = reinterpret_cast<const Real*>(a.pgrad) + d.pgrad_off + b;
+        // unrolled so that several loads are in flight; the additions stay in order
+#pragma unroll 8
         for (int64_t q = q0 + ty; q < q1; q += RY) acc += double(pg[q * d.n_branch]);
     }
     red[ty][tx] = acc;
@@ -52,26 +66,32 @@ __global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
     if (ty == 0 && b < d.n_branch) {
         double s = 0.0;
         for (int y = 0; y < RY; ++y) s += red[y][tx];
-        part[gridDim.y + d.grad_off + b] = s;
+        part[a.n_inst + d.grad_off + b] = s;
     }
 }
 
+// Pass 2: block (x, i) adds, for entries x*256 .. of instance i (entry 0: its
+// log-likelihood, entry 1 + b: branch b's gradient), its splits in z order.
 __global__ void reduce_pass2(const ReduceArgs a) {
-    const int64_t n = int64_t(a.n_inst) + (a.want_grad ? a.total_branch : 0);
-    const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (e >= n) return;
+    const int i = int(blockIdx.y);
+    const InstanceDesc& d = a.inst[i];
+    const int k = int(blockIdx.x) * int(blockDim.x) + int(threadIdx.x);
+    if (k > (a.want_grad ? d.n_branch : 0)) return;
+    const int64_t e = k == 0 ? int64_t(i) : int64_t(a.n_inst) + d.grad_off + (k - 1);
+    const int Z = red_splits(int64_t(a.C) * d.n_blocks, a.n_split);
     const int64_t stride = a.total_branch + a.n_inst;
     double s = 0.0;
-    for (int z = 0; z < a.n_split; ++z) s += a.part[int64_t(z) * stride + e];
+    for (int z = 0; z < Z; ++z) s += a.part[int64_t(z) * stride + e];
     a.out[e] = s;
 }
 
 int reduce_launches(int n_split) { return n_split > 1 ? 2 : 1; }
 
 cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStream_t st) {
-    dim3 grid(unsigned((max_branch + 31) / 32 + 1), unsigned(a.n_inst), unsigned(a.n_split));
-    dim3 block(32, RY);
-    // one split: the first pass's sums are the results (its row layout is the output's)
+    const dim3 grid(unsigned(std::max(1, a.red_blocks)));
+    const dim3 block(32, RY);
+    // at most one split per instance: the first pass's sums are the results (its row
+    // layout is the output's)
     ReduceArgs a1 = a;
     if (a.n_split == 1) a1.part = a.out;
     if (f64)
@@ -80,8 +100,8 @@ cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStr
         reduce_pass1<float><<<grid, block, 0, st>>>(a1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || a.n_split == 1) return e;
-    const int64_t n = int64_t(a.n_inst) + a.total_branch;
-    reduce_pass2<<<unsigned((n + 255) / 256), 256, 0, st>>>(a);
+    const dim3 grid2(unsigned((max_branch + 1 + 255) / 256), unsigned(a.n_inst));
+    reduce_pass2<<<grid2, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -247,9 +247,10 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
     if constexpr (FUSED) {
         // the last CTA to finish sums the partials of every item, in the order of the
         // regular reduction (reduce_pass1/2, kernels_common.cu), so that one launch and
-        // three give the same bits: per split of the items, eight strided partial sums
-        // per branch added in order; for logL, 256 strided sums, a shuffle tree per
-        // 32 of them and the eight tree sums in order; then the splits in order
+        // three give the same bits: per split of the items (red_splits of them, each a
+        // contiguous range), eight strided partial sums per branch added in order; for
+        // logL, 256 strided sums, a shuffle tree per 32 of them and the eight tree sums
+        // in order; then the splits in order
         __shared__ int last;
         __threadfence();
         __syncthreads();
@@ -264,10 +265,11 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
         for (int i = 0; i < a.n_inst; ++i) {
             const InstanceDesc d = a.inst[i];
             const int64_t n_items = int64_t(C) * d.n_blocks;
-            const int64_t per = (n_items + a.n_split - 1) / a.n_split;
+            const int Z = red_splits(n_items, a.n_split);
+            const int64_t per = (n_items + Z - 1) / Z;
             // logL: 256 strided sums per split (warp w takes strided groups w, w + W, ..)
             double tot = 0.0;
-            for (int z = 0; z < a.n_split; ++z) {
+            for (int z = 0; z < Z; ++z) {
                 const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
                 for (int y = w; y < RY; y += W) {
                     double acc = 0.0;
@@ -292,7 +294,7 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
             for (int b0 = 0; b0 < d.n_branch; b0 += CB) {
                 const int b = b0 + bi;
                 double gtot = 0.0;
-                for (int z = 0; z < a.n_split; ++z) {
+                for (int z = 0; z < Z; ++z) {
                     const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
                     if (bi < CB && b < d.n_branch) {
                         const Real* pg = pgrad + d.pgrad_off + b;

@@ -48,6 +48,7 @@ struct alignas(16) InstanceDesc {
     int32_t n_blocks;    // S_pad / site block
     int32_t pre_slots;   // stack depth of this instance (both sweeps)
     int32_t ambig;       // 1: some leaf code allows more than one but not all states
+    int32_t red_off;     // first block of this instance in the reduction's first pass
     int64_t sched_off;   // into the schedule array (SchedNode units)
     int64_t rec_off;     // into the step-record table (bytes); records are [rate][step]
     int64_t leaf_off;    // into the code table (code units) or dense table (Real units)
@@ -85,6 +86,18 @@ inline MCPHY_HOST_DEVICE int64_t param_size(int K, int Kp, int C) {
 }
 inline MCPHY_HOST_DEVICE int64_t param_m_off(int K, int Kp, int C) { return 2 * K * K + K + 1 + C + Kp; }
 inline MCPHY_HOST_DEVICE int64_t param_q_off(int K, int Kp, int C) { return 3 * K * K + K + 1 + C + Kp; }
+
+// The deterministic reduction of per-item partial sums (kernels_common.cu, and the
+// single-launch level sweep's last CTA): an instance's items are summed in
+// red_splits() contiguous ranges of at most 128 items (capped by the handle's n_split),
+// and the first pass gives each range red_groups() blocks: one per 32 branches, then
+// one for the log-likelihood.
+constexpr int RED_ITEMS = 128;
+inline MCPHY_HOST_DEVICE int red_splits(int64_t n_items, int n_split) {
+    const int64_t z = (n_items + RED_ITEMS - 1) / RED_ITEMS;
+    return int(z < 1 ? 1 : z > n_split ? n_split : z);
+}
+inline MCPHY_HOST_DEVICE int red_groups(int n_branch) { return (n_branch + 31) / 32 + 1; }
 
 enum DirtyBits : unsigned {
     DIRTY_LAYOUT = 1u,   // schedule/offsets/buffer sizes changed

@@ -267,6 +267,7 @@ extern "C" int mcphy_logpdf_grad_noalloc(mcphy_handle h, const double* d_blen_pa
     r.n_inst = int32_t(h->M);
     r.C = h->C / h->rpw;   // work items per site block
     r.n_split = h->n_split;
+    r.red_blocks = h->red_blocks;
     r.want_grad = 1;
     r.total_branch = h->total_branch;
     r.pgrad = a.pgrad;
