@@ -333,10 +333,11 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                          Real (&Y1)[SPT][KP]) -> bool {
             const unsigned js = unsigned(j) % unsigned(CH);   // slot of step j in its chunk
             if (h[3] >= 0) read_vec<KP, SPT>(stack_ptr(h[3]), lane, pb);   // else carried
+            // leaf codes of both operands (an internal operand's entries are unused)
             uint32_t c0[SPS], c1[SPS];
             const unsigned char* tj = st.tip(j, 0);
-            if (h[0] < 0) read_rows<KP, SPS>(tj, lane, c0);
-            if (h[1] < 0) read_rows<KP, SPS>(tj + St::TIP / 2, lane, c1);
+            read_rows<KP, SPS>(tj, lane, c0);
+            read_rows<KP, SPS>(tj + St::TIP / 2, lane, c1);
             // operands of the next step, one step ahead
             if (j > 0) {
                 const int qn = int(unsigned(j - 1) / unsigned(CH));
@@ -359,6 +360,31 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
             // sum_k pb_k D0_k D1_k is the same for both children, computed once
             constexpr bool kSharedDen = Pairs<Real, KP>::value;
             Real den[kSharedDen ? SPT : 1];
+            // this lane's gradient terms of branch c: sum over its slots of
+            // weight * (pt . dD) / (pt . D_c)
+            auto grad_terms = [&](const Real (&pt)[SPT][KP], const Real (&dD)[SPT][KP],
+                                  const Real (&Dc)[SPT][KP]) -> Real {
+                Real g = Real(0);
+#pragma unroll
+                for (int u = 0; u < SPT; ++u) {
+                    if constexpr (kSharedDen) {
+                        Real n0 = Real(0), n1 = Real(0);
+#pragma unroll
+                        for (int k = 0; k < KP; k += 2)
+                            fma2(pt[u][k], pt[u][k + 1], dD[u][k], dD[u][k + 1], n0, n1);
+                        g = fma(wtr[u], den_apply(n0 + n1, den[u]), g);
+                    } else {
+                        Real num = Real(0), dn = Real(0);
+#pragma unroll
+                        for (int k = 0; k < KP; ++k) {
+                            num = fma(pt[u][k], dD[u][k], num);
+                            dn = fma(pt[u][k], Dc[u][k], dn);
+                        }
+                        g = fma(wtr[u], ratio(num, dn), g);
+                    }
+                }
+                return g;
+            };
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 // pre-order partial at the top of branch c: mother's pre times the
@@ -366,7 +392,7 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 Real pt[SPT][KP];
                 vmul<KP, SPT>(pt, pb, c == 0 ? D1 : D0);
                 if constexpr (kSharedDen) {
-                    if (c == 0 && (h[4] >= 0 || h[5] >= 0)) {
+                    if (c == 0) {
 #pragma unroll
                         for (int u = 0; u < SPT; ++u) {
                             Real s0 = Real(0), s1 = Real(0);
@@ -377,33 +403,15 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                         }
                     }
                 }
-                if (h[4 + c] >= 0) {   // real branch: gradient entry h[4 + c]
-                    Real dD[SPT][KP];
-                    if (h[c] >= 0) qmat(c == 0 ? D0 : D1, dD);
-                    else look(rj, 2 * c + 1, c == 0 ? c0 : c1, dD);
-                    Real g = Real(0);
-#pragma unroll
-                    for (int u = 0; u < SPT; ++u) {
-                        if constexpr (kSharedDen) {
-                            Real n0 = Real(0), n1 = Real(0);
-#pragma unroll
-                            for (int k = 0; k < KP; k += 2)
-                                fma2(pt[u][k], pt[u][k + 1], dD[u][k], dD[u][k + 1], n0, n1);
-                            g = fma(wtr[u], den_apply(n0 + n1, den[u]), g);
-                        } else {
-                            const Real (&Dc)[SPT][KP] = c == 0 ? D0 : D1;
-                            Real num = Real(0), dn = Real(0);
-#pragma unroll
-                            for (int k = 0; k < KP; ++k) {
-                                num = fma(pt[u][k], dD[u][k], num);
-                                dn = fma(pt[u][k], Dc[u][k], dn);
-                            }
-                            g = fma(wtr[u], ratio(num, dn), g);
-                        }
-                    }
-                    gsum[c] = g;
-                }
+                // the gradient term of branch c is formed for every child: a virtual
+                // (identity) branch has entry h[4 + c] = -1 and its lanes' sum is never
+                // stored.  One branch per child: an internal child's dP L is Q_r D_c and
+                // its pre-order partial P_c^T pt follows; a leaf's dP L is a table row.
+                const Real (&Dc)[SPT][KP] = c == 0 ? D0 : D1;
+                Real dD[SPT][KP];
                 if (h[c] >= 0) {
+                    qmat(Dc, dD);
+                    gsum[c] = grad_terms(pt, dD, Dc);
                     uint32_t unused[SPT] = {};
                     if (c == 1) {
                         // child 1 is the next step: its pre-order partial is the next pb
@@ -415,9 +423,12 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                         rescale_warp<KP, Real, SPT>(pbc, unused);
                         write_vec<KP, SPT>(stack_ptr(h[2]), lane, pbc);
                     }
+                } else {
+                    look(rj, 2 * c + 1, c == 0 ? c0 : c1, dD);
+                    gsum[c] = grad_terms(pt, dD, Dc);
                 }
             }
-            if (h[4] >= 0 || h[5] >= 0) {
+            {
                 // both children's warp sums in one shuffle tree: lanes 0-15 add child
                 // 0's terms, lanes 16-31 child 1's (the same pairs, in the same order,
                 // as a warp_sum of each)
