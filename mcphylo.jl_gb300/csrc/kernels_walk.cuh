@@ -21,6 +21,8 @@
 // src/Likelihood/VectorizedFunctions.jl:2-213.)
 #pragma once
 
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace mcphy {
@@ -223,19 +225,18 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
         // ---------------- post-order sweep (logL)
         // chunk by chunk: one wait before a chunk's steps, its buffers refilled (with
         // the chunk after next) once its last step is done; record and leaf-code
-        // pointers advance by one step's bytes
+        // pointers advance by one step's bytes.  Instantiated with and without the
+        // gradient (WG: the Down vectors go to the post column), and the root step,
+        // which ends the last chunk, is taken out of the step loop.
         uint32_t eacc[SPT];
 #pragma unroll
         for (int u = 0; u < SPT; ++u) eacc[u] = 0u;
         double ll_lane = 0.0;
         Real Lp[SPT][KP];          // the previous step's partial (operand 1 of the next step)
-        for (int q = 0; q < st.Q; ++q) {
-            if (!st.wait(q)) break;
-            const unsigned char* rj = st.rec(q * CH);
-            const unsigned char* tj = st.tip(q * CH, 0);
-            const int jend = min(J, q * CH + CH);
-            for (int j = q * CH; j < jend; ++j, rj += St::BYTES, tj += St::TIP) {
-                int h[8];
+        auto post_sweep = [&](auto wg) {
+            constexpr bool WG = decltype(wg)::value;
+            // one post-order step (record rj, leaf codes tj): its partial into Lp
+            auto step = [&](const unsigned char* rj, const unsigned char* tj, int (&h)[8]) {
                 rec_header(rj, h);
                 // the post-order column keeps, for every internal child, its Down vector
                 // D_c = P_c L_c (read back by the gradient sweep instead of recomputed)
@@ -244,28 +245,39 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                     Real A[SPT][KP];
                     read_vec<KP, SPT>(stack_ptr(h[6]), lane, A);
                     mat(rj, 0, A, D0);
-                    if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, D0);
+                    if constexpr (WG) write_vec<KP, SPT>(post + int64_t(h[0]) * SLOT, lane, D0);
                 } else {
                     uint32_t c[SPS];
                     read_rows<KP, SPS>(tj, lane, c);
                     look(rj, 0, c, D0);
                 }
-                {
-                    Real D1[SPT][KP];
-                    if (h[1] >= 0) {
-                        mat(rj, 2, Lp, D1);
-                        if (a.want_grad) write_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, D1);
-                    } else {
-                        uint32_t c[SPS];
-                        read_rows<KP, SPS>(tj + St::TIP / 2, lane, c);
-                        look(rj, 2, c, D1);
-                    }
-                    vmul<KP, SPT>(Lp, D0, D1);
-                }
-                rescale_warp<KP, Real, SPT>(Lp, eacc);
-                if (j + 1 < J) {
-                    if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Lp);
+                Real D1[SPT][KP];
+                if (h[1] >= 0) {
+                    mat(rj, 2, Lp, D1);
+                    if constexpr (WG) write_vec<KP, SPT>(post + int64_t(h[1]) * SLOT, lane, D1);
                 } else {
+                    uint32_t c[SPS];
+                    read_rows<KP, SPS>(tj + St::TIP / 2, lane, c);
+                    look(rj, 2, c, D1);
+                }
+                vmul<KP, SPT>(Lp, D0, D1);
+                rescale_warp<KP, Real, SPT>(Lp, eacc);
+            };
+            for (int q = 0; q < st.Q; ++q) {
+                if (!st.wait(q)) return;
+                const unsigned char* rj = st.rec(q * CH);
+                const unsigned char* tj = st.tip(q * CH, 0);
+                const int jend = min(J, q * CH + CH);
+                const int jstop = min(J - 1, jend);   // the chunk's steps before the root
+                for (int j = q * CH; j < jstop; ++j, rj += St::BYTES, tj += St::TIP) {
+                    int h[8];
+                    step(rj, tj, h);
+                    if (h[7] >= 0) write_vec<KP, SPT>(stack_ptr(h[7]), lane, Lp);
+                }
+                if (jend == J) {
+                    // the root step: site log-likelihoods
+                    int h[8];
+                    step(rj, tj, h);
 #pragma unroll
                     for (int u = 0; u < SPT; ++u) {
                         Real lik = Real(0);
@@ -279,11 +291,13 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                         ll_lane += valid ? w * v : 0.0;
                     }
                 }
+                // chunk finished: refill its buffers with the chunk after next
+                __syncwarp();
+                if (q + 2 < st.Q) st.issue(q + 2, lane);
             }
-            // chunk finished: refill its buffers with the chunk after next
-            __syncwarp();
-            if (q + 2 < st.Q) st.issue(q + 2, lane);
-        }
+        };
+        if (a.want_grad) post_sweep(std::integral_constant<bool, true>());
+        else post_sweep(std::integral_constant<bool, false>());
         if (!st.ok) break;
         ll_lane = warp_sum(ll_lane);
         if (lane == 0) a.pll[item] = ll_lane;
