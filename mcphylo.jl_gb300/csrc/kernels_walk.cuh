@@ -352,18 +352,22 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
             const unsigned char* tj = st.tip(j, 0);
             read_rows<KP, SPS>(tj, lane, c0);
             read_rows<KP, SPS>(tj + St::TIP / 2, lane, c1);
-            // operands of the next step, one step ahead
-            if (j > 0) {
-                const int qn = int(unsigned(j - 1) / unsigned(CH));
+            // operands of the next step, one step ahead (the last step, j = 0, reloads its
+            // own: step max(j - 1, 0), whose chunk has been waited for, so no branch)
+            {
+                const int jn = j > 0 ? j - 1 : 0;
+                const int qn = int(unsigned(jn) / unsigned(CH));
                 if (qn < low) {
                     if (!st.wait(qn)) return false;
                     low = qn;
                     prefetch_chunk(qn * CH, qn * CH + CH, false);
                 }
-                rjn = st.rec(j - 1);
+                rjn = st.rec(jn);
                 rec_header(rjn, hn);
-                if (hn[0] >= 0) read_vec<KP, SPT>(post + int64_t(hn[0]) * SLOT, lane, Y0);
-                if (hn[1] >= 0) read_vec<KP, SPT>(post + int64_t(hn[1]) * SLOT, lane, Y1);
+                // a leaf operand loads post slot 0 instead (in bounds, overwritten by its
+                // table lookup), so the loads need no branch
+                read_vec<KP, SPT>(post + int64_t(max(hn[0], 0)) * SLOT, lane, Y0);
+                read_vec<KP, SPT>(post + int64_t(max(hn[1], 0)) * SLOT, lane, Y1);
             }
             if (h[0] < 0) look(rj, 0, c0, X0);
             if (h[1] < 0) look(rj, 2, c1, X1);
