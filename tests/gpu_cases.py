@@ -39,6 +39,26 @@ def caterpillar(n_taxa: int, rng, mean=0.1) -> Node:
     return root
 
 
+def balanced(depth: int, rng, mean=0.1) -> Node:
+    """A perfectly balanced binary tree of 2**depth leaves (the deepest partial stacks
+    a tree of that size can need)."""
+    count = [0]
+
+    def grow(d):
+        if d == 0:
+            count[0] += 1
+            return Node(f"t{count[0]}")
+        n = Node()
+        for _ in range(2):
+            c = n.add_child(grow(d - 1))
+            c.inc_length = rng.exponential(mean)
+        return n
+
+    root = grow(depth)
+    number_nodes(root)
+    return root
+
+
 def random_instance(K, C, taxa, S, seed, multifurcate=0.0, missing=0.05, tree=None,
                     model="gtr"):
     rng = np.random.default_rng(seed)

@@ -4,7 +4,7 @@ import pytest
 
 from conftest import load_alignment
 from gpu_cases import (F32_G_FLOOR, F32_G_RTOL, F32_LL_RTOL, F64_G_FLOOR, F64_G_RTOL, F64_RTOL,
-                       assert_grad_close, caterpillar, engine, level_fits, oracle, oracle_ll,
+                       assert_grad_close, balanced, caterpillar, engine, level_fits, oracle, oracle_ll,
                        random_instance)
 
 import mcphylo_gb300 as mp
@@ -751,3 +751,23 @@ def test_two_engines_on_two_host_threads(built_lib):
         assert len(out[k]) == 20
         for ll, g in out[k]:
             assert ll == alone[k][0] and np.array_equal(g, alone[k][1])
+
+
+@pytest.mark.parametrize("spt", [1, 2, 4])
+def test_deep_stack_in_global_slots(built_lib, spt):
+    """The tree walk keeps the first stack slots of a warp in shared memory and deeper
+    ones in its global column: a balanced 256-leaf tree needs more slots than shared
+    memory holds at every sites-per-thread shape, a 40-taxon Yule tree fits.  Both
+    against the oracle."""
+    rng = np.random.default_rng(31)
+    shallow = random_instance(4, 4, 40, 700, seed=32)
+    deep = random_instance(4, 4, 0, 300, seed=33, tree=balanced(8, rng))
+    assert mp.schedule_info(deep.parent)["pre_slots"] > 6
+    for inst in (shallow, deep):
+        llo, go = oracle(inst)
+        e = engine(inst, "f32", spt)
+        e.set_sweep("walk")
+        ll, g = e.logpdf_grad()
+        e.close()
+        assert abs(ll - llo) <= F32_LL_RTOL * abs(llo), (ll, llo)
+        assert_grad_close(g, go, F32_G_RTOL, F32_G_FLOOR)
