@@ -455,10 +455,9 @@ __global__ void __launch_bounds__(256) prune_rows_kernel(const PruneArgs a) {
                 v += __shfl_xor_sync(0xffffffffu, hi ? gsum[0] : gsum[1], 16);
 #pragma unroll
                 for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                if (unsigned(lane & 15) == js) {
-                    gstash = v;
-                    gidx = hi ? h[5] : h[4];
-                }
+                const bool mine = unsigned(lane & 15) == js;   // selects, not a branch
+                gstash = mine ? v : gstash;
+                gidx = mine ? (hi ? h[5] : h[4]) : gidx;
             }
             // chunk finished (descending): its gradient entries out, its buffers
             // refilled two chunks below
