@@ -1035,8 +1035,10 @@ __host__ __device__ constexpr int rec_row_threads(int kp) { return kp >= 8 ? kp 
 // Part (child c, rows s0, s0 + R, ..) of the record of schedule step j (node sn) of
 // instance d for rate r, written at rec; the (c == 0, s0 == 0) part also writes the
 // header.  Shared by the global record build and the fused small-problem sweep, so
-// both give the same bits.
-template <typename Real>
+// both give the same bits.  KPT > 0: the state-space padding Kp known at compile time
+// (2 or 4, where one thread builds every row: s0 = 0, R = 1; every loop unrolls and the
+// exponentials stay in registers); 0: any Kp.
+template <typename Real, int KPT = 0>
 __device__ __forceinline__ void build_record_part(unsigned char* rec, const SchedNode& sn,
                                                   const SchedNode* sched, const InstanceDesc& d,
                                                   const double* params, const double* blen, int j,
@@ -1087,37 +1089,76 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
     // in the off-diagonal entries of short branches (t ~ 1e-5); dP/dt =
     // U diag(D r mu exp(x)) Uinv as the reference forms it
     const double* Mu = params + d.param_off + param_m_off(K, Kp, C);
-    double em[32], de[32];
-    if (s0 < K)
-        for (int m = 0; m < K; ++m) {
-            const double x = mu * t * Dv[m] * rate;
-            em[m] = expm1(x);
-            de[m] = Dv[m] * rate * mu * (1.0 + em[m]);   // exp(x), one transcendental
+    // the exponentials, then row s of P and dP (and their row sums); with KPT the loops
+    // run over the compile-time padding (unrolled, the arrays in registers) and stop at
+    // K, the same operations in the same order as the general loops
+    constexpr int KM = KPT > 0 ? KPT : 32;        // most states
+    double em[KM], de[KM];
+    auto exps = [&](int m) {
+        const double x = mu * t * Dv[m] * rate;
+        em[m] = expm1(x);
+        de[m] = Dv[m] * rate * mu * (1.0 + em[m]);   // exp(x), one transcendental
+    };
+    if constexpr (KPT > 0) {
+        if (s0 < K) {
+#pragma unroll
+            for (int m = 0; m < KPT; ++m)
+                if (m < K) exps(m);
         }
-    for (int s = s0; s < Kp; s += R) {
-        double rs = 0.0, drs = 0.0;
-        for (int k = 0; k < Kp; ++k) {
-            double p = 0.0, dp = 0.0;
-            if (s < K && k < K) {
-                for (int m = 0; m < K; ++m) {
-                    p += U[s + K * m] * em[m] * Uinv[m + K * k];
-                    dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+#pragma unroll
+        for (int s = 0; s < KPT; ++s) {
+            double rs = 0.0, drs = 0.0;
+#pragma unroll
+            for (int k = 0; k < KPT; ++k) {
+                double p = 0.0, dp = 0.0;
+                if (s < K && k < K) {
+#pragma unroll
+                    for (int m = 0; m < KPT; ++m) {
+                        if (m < K) {
+                            p += U[s + K * m] * em[m] * Uinv[m + K * k];
+                            dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+                        }
+                    }
+                    p += Mu[s + K * k];
+                    rs += p;
+                    drs += dp;
+                } else {
+                    p = (s == k) ? 1.0 : 0.0;
                 }
-                p += Mu[s + K * k];
-                rs += p;
-                drs += dp;
-            } else {
-                p = (s == k) ? 1.0 : 0.0;
+                PT[k * KPT + s] = Real(p);
+                dPT[k * KPT + s] = Real(dp);
             }
-            PT[k * Kp + s] = Real(p);
-            dPT[k * Kp + s] = Real(dp);
+            PT[KPT * KPT + s] = Real(rs);
+            dPT[KPT * KPT + s] = Real(drs);
         }
-        PT[Kp * Kp + s] = Real(rs);
-        dPT[Kp * Kp + s] = Real(drs);
+    } else {
+        if (s0 < K)
+            for (int m = 0; m < K; ++m) exps(m);
+        for (int s = s0; s < Kp; s += R) {
+            double rs = 0.0, drs = 0.0;
+            for (int k = 0; k < Kp; ++k) {
+                double p = 0.0, dp = 0.0;
+                if (s < K && k < K) {
+                    for (int m = 0; m < K; ++m) {
+                        p += U[s + K * m] * em[m] * Uinv[m + K * k];
+                        dp += U[s + K * m] * de[m] * Uinv[m + K * k];
+                    }
+                    p += Mu[s + K * k];
+                    rs += p;
+                    drs += dp;
+                } else {
+                    p = (s == k) ? 1.0 : 0.0;
+                }
+                PT[k * Kp + s] = Real(p);
+                dPT[k * Kp + s] = Real(dp);
+            }
+            PT[Kp * Kp + s] = Real(rs);
+            dPT[Kp * Kp + s] = Real(drs);
+        }
     }
 }
 
-template <typename Real>
+template <typename Real, int KPT = 0>
 __global__ void build_records_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, Kp = a.Kp, C = a.C;
@@ -1136,7 +1177,45 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const int j = sj.y;
     const SchedNode sn = a.sched[d.sched_off + j];
     unsigned char* rec = a.recs + d.rec_off + rec_index(r, j, d.J, a.rpw) * size_t(rec_bytes(Kp, sizeof(Real)));
-    build_record_part<Real>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, C, r, c, s0, R);
+    build_record_part<Real, KPT>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, C, r, c, s0, R);
+}
+
+// Two and four states: a block of 128 threads builds the records of 64 consecutive
+// steps (two children each) of one rate category in shared memory, then writes them out
+// as 16-byte stores, so that consecutive threads write consecutive bytes of a record
+// (records of one instance and rate are contiguous by step).  The same record parts
+// as build_records_kernel, the same bits.
+constexpr int REC_TILE_STEPS = 64;
+template <typename Real, int KPT>
+__global__ void __launch_bounds__(2 * REC_TILE_STEPS) build_records_tiled_kernel(const BuildRecArgs a) {
+    constexpr int RB = rec_bytes(KPT, sizeof(Real));
+    static_assert(RB % 16 == 0, "records are whole 16-byte words");
+    __shared__ __align__(16) unsigned char srec[REC_TILE_STEPS * RB];
+    const int r = int(blockIdx.y);
+    const int64_t g0 = int64_t(blockIdx.x) * REC_TILE_STEPS;
+    const int t = int(threadIdx.x);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && t == 0 && a.counter) {
+        a.counter[0] = 0;
+        a.counter[1] = 0;
+    }
+    const int n = int(min(int64_t(REC_TILE_STEPS), int64_t(a.n_steps) - g0));
+    const int i = t >> 1, c = t & 1;
+    if (i < n) {
+        const int2 sj = a.steps[g0 + i];
+        const InstanceDesc& d = a.inst[sj.x];
+        const SchedNode sn = a.sched[d.sched_off + sj.y];
+        build_record_part<Real, KPT>(srec + size_t(i) * RB, sn, a.sched + d.sched_off, d, a.params, a.blen,
+                                     sj.y, a.K, KPT, a.C, r, c, 0, 1);
+    }
+    __syncthreads();
+    constexpr int Q = RB / 16;
+    for (int e = t; e < n * Q; e += blockDim.x) {
+        const int ii = e / Q, w = e - ii * Q;
+        const int2 sj = a.steps[g0 + ii];
+        const InstanceDesc& d = a.inst[sj.x];
+        unsigned char* dst = a.recs + d.rec_off + rec_index(r, sj.y, d.J, a.rpw) * size_t(RB);
+        reinterpret_cast<int4*>(dst)[w] = reinterpret_cast<const int4*>(srec + size_t(ii) * RB)[w];
+    }
 }
 
 // ---------------------------------------------------------------- reduction

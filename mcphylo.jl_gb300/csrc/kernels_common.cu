@@ -106,6 +106,20 @@ cudaError_t launch_reduce(bool f64, const ReduceArgs& a, int max_branch, cudaStr
 }
 
 cudaError_t launch_build_records(bool f64, const BuildRecArgs& a, cudaStream_t st) {
+    // two and four states: records built in shared memory a tile of steps at a time
+    // and written out contiguously
+    if ((a.Kp == 2 || a.Kp == 4) && a.n_steps > 0) {
+        const dim3 grid(unsigned((int64_t(a.n_steps) + REC_TILE_STEPS - 1) / REC_TILE_STEPS), unsigned(a.C));
+        const int tpb = 2 * REC_TILE_STEPS;
+        if (f64) {
+            if (a.Kp == 2) build_records_tiled_kernel<double, 2><<<grid, tpb, 0, st>>>(a);
+            else build_records_tiled_kernel<double, 4><<<grid, tpb, 0, st>>>(a);
+        } else {
+            if (a.Kp == 2) build_records_tiled_kernel<float, 2><<<grid, tpb, 0, st>>>(a);
+            else build_records_tiled_kernel<float, 4><<<grid, tpb, 0, st>>>(a);
+        }
+        return cudaGetLastError();
+    }
     // at least one thread: it also zeroes the sweep's counter
     const int64_t total = std::max<int64_t>(1, int64_t(a.n_steps) * 2 * a.C * rec_row_threads(a.Kp));
     const int tpb = 128;

@@ -104,8 +104,10 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
                 const SchedNode* sc = a.sched + d.sched_off;
                 for (int q = threadIdx.x; q < J * 2 * R; q += blockDim.x) {
                     const int s0 = q % R, c = (q / R) % 2, j = q / (2 * R);
-                    build_record_part<Real>(srec + size_t(j) * RB, sc[j], sc, d, a.params, a.blen, j,
-                                            a.K, KP, C, r, c, s0, R);
+                    // the instantiation the record kernel runs for this padding (same bits)
+                    build_record_part<Real, (KP <= 4 ? KP : 0)>(srec + size_t(j) * RB, sc[j], sc, d,
+                                                                a.params, a.blen, j, a.K, KP, C, r, c,
+                                                                s0, R);
                 }
             } else {
                 const int4* src = reinterpret_cast<const int4*>(a.recs + d.rec_off + size_t(r) * J * RB);
