@@ -246,7 +246,7 @@ def cpu_leg(args):
            args.workload, "--steps", str(args.cpu_steps), "--warmup", "3", "--ref-units",
            str(args.ref_units)]
     env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
-    p = subprocess.run(cmd, capture_output=True, text=True, env=env,
+    p = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1800,
                        cwd=os.path.dirname(os.path.abspath(__file__)))
     if p.returncode != 0:
         raise RuntimeError("cpu_baseline leg failed: " + p.stderr[-2000:])
