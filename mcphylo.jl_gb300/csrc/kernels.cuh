@@ -1218,6 +1218,29 @@ __global__ void __launch_bounds__(2 * REC_TILE_STEPS) build_records_tiled_kernel
     }
 }
 
+// Running sum of item partials for the reduction.  FP64 partials add in FP64.  FP32
+// partials add as an unevaluated FP32 pair (value + error, Knuth's TwoSum: about 48
+// significant bits, the rounding of each addition kept exactly in the error term), since
+// converting every FP32 partial to FP64 and adding in FP64 runs at GB300's FP64 rate; the
+// pair becomes one FP64 value at the end.
+template <typename Real> struct ItemSum;
+template <> struct ItemSum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct ItemSum<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x);
+        const float bb = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
 // ---------------------------------------------------------------- reduction
 // Per (instance, branch) FP64 sums of the item partials, in two passes with a
 // fixed summation order (kernels_common.cu).

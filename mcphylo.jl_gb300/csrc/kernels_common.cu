@@ -58,8 +58,10 @@ __global__ void __launch_bounds__(32 * RY) reduce_pass1(const ReduceArgs a) {
     if (b < d.n_branch) {
         const Real* pg = reinterpret_cast<const Real*>(a.pgrad) + d.pgrad_off + b;
         // unrolled so that several loads are in flight; the additions stay in order
+        ItemSum<Real> sum;
 #pragma unroll 8
-        for (int64_t q = q0 + ty; q < q1; q += RY) acc += double(pg[q * d.n_branch]);
+        for (int64_t q = q0 + ty; q < q1; q += RY) sum.add(pg[q * d.n_branch]);
+        acc = sum.value();
     }
     red[ty][tx] = acc;
     __syncthreads();

@@ -300,10 +300,10 @@ __global__ void __launch_bounds__(256, 1) prune_level_kernel(const PruneArgs a) 
                     const int64_t q0 = int64_t(z) * per, q1 = min(n_items, q0 + per);
                     if (bi < CB && b < d.n_branch) {
                         const Real* pg = pgrad + d.pgrad_off + b;
-                        double acc = 0.0;
+                        ItemSum<Real> sum;
 #pragma unroll 4
-                        for (int64_t q = q0 + y; q < q1; q += RY) acc += double(__ldcg(pg + q * d.n_branch));
-                        red[y * CB + bi] = acc;
+                        for (int64_t q = q0 + y; q < q1; q += RY) sum.add(__ldcg(pg + q * d.n_branch));
+                        red[y * CB + bi] = sum.value();
                     }
                     __syncthreads();
                     if (int(threadIdx.x) < CB && b0 + int(threadIdx.x) < d.n_branch) {
