@@ -1158,7 +1158,7 @@ __device__ __forceinline__ void build_record_part(unsigned char* rec, const Sche
     }
 }
 
-template <typename Real, int KPT = 0>
+template <typename Real>
 __global__ void build_records_kernel(const BuildRecArgs a) {
     const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const int K = a.K, Kp = a.Kp, C = a.C;
@@ -1177,7 +1177,7 @@ __global__ void build_records_kernel(const BuildRecArgs a) {
     const int j = sj.y;
     const SchedNode sn = a.sched[d.sched_off + j];
     unsigned char* rec = a.recs + d.rec_off + rec_index(r, j, d.J, a.rpw) * size_t(rec_bytes(Kp, sizeof(Real)));
-    build_record_part<Real, KPT>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, C, r, c, s0, R);
+    build_record_part<Real>(rec, sn, a.sched + d.sched_off, d, a.params, a.blen, j, K, Kp, C, r, c, s0, R);
 }
 
 // Two and four states: a block of 128 threads builds the records of 64 consecutive
