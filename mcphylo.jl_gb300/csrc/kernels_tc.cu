@@ -12,9 +12,9 @@
 //     D_c = L_c P_c^T (MMA for internal c), L = D_0 * D_1, power-of-two rescale,
 //     written to the CTA's global column [step][state][128 sites];
 //   pre-order (gradient, LikelihoodCalculator_Node.jl:3-78):
-//     round 1: D_c = L_c P_c^T and dD_c = L_c dP_c^T (MMAs for internal c);
+//     MMA round 1: D_c = L_c P_c^T and dD_c = L_c dP_c^T (MMAs for internal c);
 //     pt_c = pb * D_sibling, gradient term (pt_c . dD_c) / (pt_c . D_c);
-//     round 2: pb_c = pt_c P_c (MMA for internal c), rescaled; child 1's stays in
+//     MMA round 2: pb_c = pt_c P_c (MMA for internal c), rescaled; child 1's stays in
 //     registers (it is the next step), child 0's goes to the CTA's stack column.
 // Every wait is bounded: a timeout sets the error flag, the CTA drains its copies
 // and MMAs (bounded) and frees its TMEM before it returns.
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
             failed = true;
             break;
         }
-        // round 1 of a step: D_c and dD_c of its internal children, from stage st
+        // MMA round 1 of a step: D_c and dD_c of its internal children, from stage st
         auto add_round1 = [&](int st, int& n, const unsigned char** at, const unsigned char** bt,
                               uint32_t* dc) {
             const unsigned char* Rs = rec(st);
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(TC_M, 1) prune_tc_kernel(const PruneArgs a) {
                 red[(b * 4 + warp) * 2 + 0] = g0;
                 red[(b * 4 + warp) * 2 + 1] = g1;
             }
-            // step j - 1's stage must be in for its round 1
+            // step j - 1's stage must be in for its MMA round 1
             bool ok = okr;
             bool next_in = false;
             if (j > 0) {
